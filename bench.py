@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Benchmark: path segments/s of the GB300 path tracer at 1920x1080.
+
+One step = one full frame of the default-quality workload (c2_default:
+1920x1080, 1024 samples per pixel, at most 12 bounces, 64 spheres + 16 cubes
++ the ground cube, brute-force closest hit), rendered from a cleared
+accumulator with a fresh seed.  A segment is one trace_ray call of the
+reference (src/renderer/cpu.rs:257); the kernel counts them exactly.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`ours` prints one JSON line: `value` is segments/s with the scene and
+accumulator resident on the device (the timed region is bracketed by
+barrier + synchronize; the 256 MiB L2-flush write between steps is inside
+it), `e2e` is the same metric through the C ABI from host buffers (scene
+upload, reset, render, 8-bit read-back every step), `roofline` relates the
+render kernel's CUDA-event time to the FP32 issue rate measured in the same
+run, and `cpu_baseline` times the CPU oracle (single thread, like the
+reference's serial pixel loop) on a bounded sample of the same workload.
+
+`reference` times the CPU restatement of the reference renderer on all host
+threads (the reference is Rust and cannot be built here), one 1-spp frame of
+the same workload per step.
+
+With N > 1 (torchrun), every rank renders the full workload with its own
+seeds on its own GPU ("replicas", weak scaling); value = all ranks' segments
+/ the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "path segments/s @1080p"
+UNIT = "segments/s"
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--spp", type=int, default=0, help="samples per pixel per step (default: the workload's 1024)")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _workload():
+    from raydar_gb300 import scenegen
+    return scenegen.c2_default()
+
+
+def _config(w, spp):
+    n = len(w.scene.objects)
+    return {
+        "workload": f"c2_default: {w.scene.width}x{w.scene.height}, {spp} spp per step, "
+                    f"max {w.max_bounces} bounces, {n} objects (64 spheres + 16 cubes + ground), brute force",
+        "resolution": [w.scene.width, w.scene.height],
+        "spp_per_step": spp,
+        "max_bounces": w.max_bounces,
+        "objects": n,
+        "scene_seed": 2,
+        "l2": "scene and accumulator fit in L2; a 256 MiB buffer is written before every timed step to flush it",
+    }
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "power_w_max": max(power),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------ CPU baseline --
+def cpu_baseline(w, seconds: float):
+    """The oracle on one host thread over a random pixel sample of the same
+    1080p workload (1 spp, 12 bounces), sized to about `seconds` of work."""
+    import numpy as np
+
+    import oracle
+    sc = w.scene.to_c()
+    npix = w.scene.width * w.scene.height
+    rng = np.random.default_rng(0)
+    n = 2000
+    total_seg, total_t, total_px = 0, 0.0, 0
+    while True:
+        px = rng.choice(npix, n, replace=False).astype(np.uint32)
+        t0 = time.perf_counter()
+        _, seg = oracle.render_pixels(sc, px, 0, 1, w.max_bounces, 7)
+        dt = time.perf_counter() - t0
+        total_seg += seg
+        total_t += dt
+        total_px += n
+        if total_t >= seconds:
+            break
+        rate = max(n / max(dt, 1e-6), 1.0)
+        n = int(min(npix, max(500, rate * (seconds - total_t) * 1.05)))
+    return {"value": total_seg / total_t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{total_px} random pixels of the 1920x1080 c2_default frame, 1 spp, "
+                      f"{w.max_bounces} bounces, {total_seg} segments in {total_t:.1f} s "
+                      f"(CPU oracle, -O2 -ffp-contract=off, one thread)"}
+
+
+# --------------------------------------------------------------- reference --
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    import oracle
+    w = _workload()
+    sc = w.scene.to_c()
+    try:
+        threads = len(os.sched_getaffinity(0))
+    except AttributeError:
+        threads = os.cpu_count() or 1
+    for i in range(args.warmup):
+        oracle.render(sc, 0, 1, w.max_bounces, 500 + i, threads=threads)
+    segs = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        _, s = oracle.render(sc, 0, 1, w.max_bounces, 1000 + k, threads=threads)
+        segs += s
+    dt = time.perf_counter() - t0
+    v = segs / dt
+    cfg = _config(w, 1)
+    cfg["workload"] = cfg["workload"].replace("1 spp per step", "1 spp per step (CPU sample of the 1024-spp frame)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded c2_default scene)", "config": cfg,
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full 1920x1080 frame at 1 spp per step on {threads} host threads: the CPU "
+                                   "restatement of src/renderer/cpu.rs (the Rust reference cannot be built here)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------------- ours --
+def _traffic_per_segment():
+    """DRAM bytes per segment of the render kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "render_kernel_traffic.json"
+    if not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+        return float(d["dram_bytes_per_segment"])
+    except (ValueError, KeyError):
+        return None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from raydar_gb300 import CudaRenderer, RendererConfig, native
+    from raydar_gb300.roofline import ops_per_segment
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    w = _workload()
+    spp = args.spp or w.spp
+    r = CudaRenderer(RendererConfig(max_sample_count=spp, max_bounces=w.max_bounces), device=local, seed=0)
+    lib, ctx = r.lib, r.ctx
+    r.upload(w.scene)
+    sptr = C.c_void_p()
+    r._check(lib.rdc_get_stream(ctx, C.byref(sptr)), "rdc_get_stream")
+    stream = torch.cuda.ExternalStream(sptr.value, device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    ops_s = C.c_double(0)
+    mhz = C.c_double(0)
+    r._check(lib.rdc_measure_fp32_issue(ctx, C.byref(ops_s), C.byref(mhz)), "rdc_measure_fp32_issue")
+
+    def render(seed):
+        r._check(lib.rdc_reset(ctx), "rdc_reset")
+        r._check(lib.rdc_render(ctx, 0, spp, w.max_bounces, seed), "rdc_render")
+
+    seed_base = 1000 + 100000 * rank
+    for i in range(args.warmup):
+        render(seed_base + 50000 + i)
+    r._check(lib.rdc_synchronize(ctx), "sync")
+
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = str(getattr(props, "uuid", "") or "")
+    gpu_id = f"GPU-{gpu_id}" if gpu_id and not gpu_id.startswith("GPU-") else (gpu_id or str(local))
+    clocks = ClockSampler(gpu_id)
+
+    evs = []
+    segs = []
+    launches = 0
+    barrier()
+    clocks.start()
+    time.sleep(0.4)
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r._check(lib.rdc_reset(ctx), "rdc_reset")
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r._check(lib.rdc_render(ctx, 0, spp, w.max_bounces, seed_base + k), "rdc_render")
+        e1.record(stream)
+        st = r.stats()  # synchronises the context stream
+        segs.append(st.segments)
+        launches += st.kernel_launches
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    barrier()
+    clk = clocks.stop()
+    elapsed = t1 - t0
+    kernel_ms = [a.elapsed_time(b) for a, b in evs]
+    my_segments = sum(segs)
+
+    if dist is not None:
+        t = torch.tensor([elapsed], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+        s = torch.tensor([my_segments], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(s, op=dist.ReduceOp.SUM)
+        total_segments = float(s.item())
+    else:
+        total_segments = float(my_segments)
+
+    # ---- e2e through the C ABI from host buffers --------------------------
+    img = np.empty((w.scene.height, w.scene.width, 4), np.uint8)
+    sc = w.scene.to_c()
+    st0 = r.stats()
+    e2e_segs = 0
+    barrier()
+    te0 = time.perf_counter()
+    for k in range(args.steps):
+        r._check(lib.rdc_scene_upload(ctx, sc.ref()), "rdc_scene_upload")
+        r._check(lib.rdc_reset(ctx), "rdc_reset")
+        r._check(lib.rdc_render(ctx, 0, spp, w.max_bounces, seed_base + 20000 + k), "rdc_render")
+        r._check(lib.rdc_read_rgba8(ctx, spp, native.u8ptr(img), img.size), "rdc_read_rgba8")
+        e2e_segs += r.stats().segments
+    te1 = time.perf_counter()
+    st1 = r.stats()
+    e2e_time = te1 - te0
+    if dist is not None:
+        t = torch.tensor([e2e_time, float(e2e_segs)], dtype=torch.float64, device=f"cuda:{local}")
+        tm = t.clone()
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e_time, e2e_total = float(tm[0].item()), float(t[1].item())
+    else:
+        e2e_total = float(e2e_segs)
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        base = cpu_baseline(w, args.cpu_seconds)
+
+    r.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+
+    n_obj = len(w.scene.objects)
+    ops = ops_per_segment(n_obj)
+    mean_kernel_s = sum(kernel_ms) / len(kernel_ms) / 1e3
+    seg_per_launch = my_segments / len(segs)
+    achieved = ops * seg_per_launch / mean_kernel_s / 1e12
+    peak = ops_s.value / 1e12
+    tps = _traffic_per_segment()
+    line = {
+        "metric": METRIC, "value": total_segments / elapsed, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded c2_default scene (64 spheres, 16 cubes, ground), fresh seed per step",
+        "config": _config(w, spp),
+        "segments_per_step": seg_per_launch,
+        "paths_per_step": w.scene.width * w.scene.height * spp,
+        "kernel_ms_per_step": sum(kernel_ms) / len(kernel_ms),
+        "roofline": {
+            "bound": "fp32", "kernel": "render_kernel", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak > 0 else None,
+            "traffic": (tps * seg_per_launch if tps is not None else None),
+            "ops_per_segment": ops,
+            "peak_source": f"measured in this run: FFMA issue rate {peak:.2f} T lane-ops/s "
+                           f"(= {mhz.value:.0f} MHz x SMs x 128), one op per lane per clock",
+        },
+        "e2e": {"value": e2e_total / e2e_time, "unit": UNIT,
+                "h2d_bytes_per_step": (st1.h2d_bytes - st0.h2d_bytes) / args.steps,
+                "d2h_bytes_per_step": (st1.d2h_bytes - st0.d2h_bytes) / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "cpu_baseline": base,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

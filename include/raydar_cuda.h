@@ -1,0 +1,243 @@
+/*
+ * raydar_cuda.h -- C ABI of the GB300 (sm_103a) path-tracing backend for Raydar.
+ *
+ * This library replaces the hot path of Raydar's CPU renderer
+ * (src/renderer/cpu.rs:193-394 with src/utils/mod.rs:6-55 and
+ * src/scene/world.rs:17-31): camera ray generation, sphere/cube closest hit,
+ * Diffuse/Specular/Metal/Glass scattering, the bounce loop and per-pixel
+ * sample accumulation.  It sits behind Raydar's `trait Renderer`
+ * (src/renderer/mod.rs:25-35); a Rust `CudaRenderer` binds these symbols.
+ *
+ * Conventions
+ *   - Every entry point returns rdc_status (0 = RDC_OK).  No exception or
+ *     panic crosses the ABI.  The message of the last failure on a context is
+ *     returned by rdc_last_error(ctx); failures of rdc_create (no context yet)
+ *     are reported by rdc_last_error(NULL) on the calling thread.
+ *   - The caller owns every host buffer; the context owns all device memory.
+ *     Host arrays passed in are copied during the call.
+ *   - A context is used from one thread at a time (the reference trait takes
+ *     `&mut self`).  The context serialises its work on its own CUDA stream.
+ *   - Matrices are column-major 4x4 float (x column first), exactly as
+ *     serialised in `.rscn` files (src/scene/camera.rs:26-29).
+ *   - Randomness is a counter-based Philox4x32-10 stream keyed by
+ *     (seed, pixel, sample, bounce), so a render is deterministic, progressive
+ *     rendering in any split of the sample range gives bit-identical results,
+ *     and the CPU oracle can replay any path.
+ */
+#ifndef RAYDAR_CUDA_H
+#define RAYDAR_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RDC_ABI_VERSION 1
+
+typedef enum rdc_status {
+    RDC_OK = 0,
+    RDC_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, malformed scene */
+    RDC_ERR_UNSUPPORTED = 2,      /* e.g. World::Transparent (a todo!() panic in the reference) */
+    RDC_ERR_LIMIT = 3,            /* a size above the documented maxima below */
+    RDC_ERR_NO_SCENE = 4,         /* render/read before rdc_scene_upload */
+    RDC_ERR_CUDA = 5,             /* a CUDA runtime call failed; see rdc_last_error */
+    RDC_ERR_OUT_OF_MEMORY = 6,
+    RDC_ERR_DEVICE = 7            /* a kernel reported an error flag (bounds/step cap) */
+} rdc_status;
+
+/* Geometry kinds: src/scene/objects.rs:6-10. */
+enum { RDC_GEOMETRY_SPHERE = 0, RDC_GEOMETRY_CUBE = 1 };
+/* World kinds: src/scene/world.rs:6-14. */
+enum { RDC_WORLD_SKY_COLOR = 0, RDC_WORLD_SOLID_COLOR = 1, RDC_WORLD_TRANSPARENT = 2 };
+/* Projection kinds: src/scene/camera.rs:8-11. */
+enum { RDC_PROJECTION_PERSPECTIVE = 0, RDC_PROJECTION_ORTHOGRAPHIC = 1 };
+
+/* Documented maxima (checked on upload; RDC_ERR_LIMIT above them). */
+#define RDC_MAX_RESOLUTION 16384u     /* per axis */
+#define RDC_MAX_OBJECTS 4096u         /* brute-force path: geometry staged in shared memory */
+#define RDC_MAX_BOUNCES 1024u
+
+/* Camera, field for field as src/scene/camera.rs:13-30.  The renderer uses
+ * `position`, the resolution and the two inverse matrices as stored; the
+ * remaining fields are carried so a caller can round-trip a Camera. */
+typedef struct rdc_camera {
+    float position[3];
+    float target[3];
+    float up[3];
+    uint32_t resolution_x;
+    uint32_t resolution_y;
+    uint32_t projection;      /* RDC_PROJECTION_* */
+    float fov_degrees;        /* Projection::Perspective { fov } */
+    float ortho_size;         /* Projection::Orthographic { size } */
+    float near_clip;
+    float far_clip;
+    float view_matrix[16];
+    float proj_matrix[16];
+    float inverse_view_matrix[16];
+    float inverse_proj_matrix[16];
+} rdc_camera;
+
+/* World, src/scene/world.rs:6-14.  SkyColor uses top/bottom; SolidColor uses
+ * solid_color; Transparent is rejected with RDC_ERR_UNSUPPORTED. */
+typedef struct rdc_world {
+    uint32_t kind;            /* RDC_WORLD_* */
+    float top_color[3];
+    float bottom_color[3];
+    float solid_color[3];
+} rdc_world;
+
+/* Material, src/scene/material.rs:4-13. */
+typedef struct rdc_material {
+    float albedo[3];
+    float roughness;
+    float metallic;
+    float emission_color[3];
+    float emission_strength;
+    float transmission;
+    float ior;
+} rdc_material;
+
+/* Object, src/scene/objects.rs:12-16 with Geometry::{Sphere,Cube} (40-50). */
+typedef struct rdc_object {
+    uint32_t geometry;        /* RDC_GEOMETRY_* */
+    float center[3];
+    float radius;             /* Sphere::radius (ignored for cubes) */
+    float side_length;        /* Cube::side_length (ignored for spheres) */
+    rdc_material material;
+} rdc_object;
+
+/* Scene, src/scene/mod.rs:13-18.  `objects` keeps the scene's own order: the
+ * closest-hit tie rule (first minimum wins, src/renderer/cpu.rs:345-349)
+ * depends on it. */
+typedef struct rdc_scene_desc {
+    rdc_camera camera;
+    rdc_world world;
+    const rdc_object* objects;
+    uint32_t object_count;
+} rdc_scene_desc;
+
+typedef struct rdc_stats {
+    uint64_t segments;        /* trace_ray calls (src/renderer/cpu.rs:257) in the last render */
+    uint64_t paths;           /* pixels x samples in the last render */
+    float device_ms;          /* CUDA-event time of the last render's kernels */
+    uint32_t sample_count;    /* samples accumulated since the last reset */
+    uint32_t kernel_launches; /* kernels launched by the last render */
+    uint64_t h2d_bytes;       /* host->device bytes the context has copied since creation */
+    uint64_t d2h_bytes;       /* device->host bytes the context has copied since creation */
+} rdc_stats;
+
+typedef struct rdc_ctx rdc_ctx;
+
+/* ---- lifetime --------------------------------------------------------- */
+
+/* Library version string. */
+const char* rdc_version(void);
+
+/* Create a context on CUDA device `device`.  Replaces constructing a renderer
+ * (CpuRenderer::new, src/renderer/cpu.rs:186; src/cli/mod.rs:50-54). */
+rdc_status rdc_create(rdc_ctx** out, int device);
+
+/* Destroy a context and free its device memory.  NULL is accepted. */
+void rdc_destroy(rdc_ctx* ctx);
+
+/* Message of the last failure on `ctx` ("" if none).  With ctx == NULL:
+ * the last rdc_create failure on the calling thread. */
+const char* rdc_last_error(const rdc_ctx* ctx);
+
+/* The CUDA stream (cudaStream_t) all of the context's work is ordered on. */
+rdc_status rdc_get_stream(rdc_ctx* ctx, void** stream_out);
+
+/* Block until all work queued on the context has finished. */
+rdc_status rdc_synchronize(rdc_ctx* ctx);
+
+/* ---- scene ------------------------------------------------------------ */
+
+/* Copy a scene to the device: validates it, flattens the objects into
+ * structure-of-arrays records and precomputes per-object constants.
+ * Replaces the `&Scene` each Renderer method receives (src/renderer/mod.rs:26-28).
+ * If the resolution changed, the accumulator is reallocated and zeroed, as
+ * CpuRenderer::frame_buffer does (src/renderer/cpu.rs:400-417). */
+rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* scene);
+
+/* ---- rendering -------------------------------------------------------- */
+
+/* Zero the RGBA accumulator and the sample count: Renderer::new_frame
+ * (src/renderer/cpu.rs:135-140, 419-423). */
+rdc_status rdc_reset(rdc_ctx* ctx);
+
+/* Trace samples [spp_begin, spp_begin + spp_count) of every pixel with at
+ * most `max_bounces` segments per path and add them, in sample order, to
+ * the accumulator: the body of CpuRenderer::render_next_sample
+ * (src/renderer/cpu.rs:193-219) repeated spp_count times, with per_pixel
+ * (233-342), trace_ray (344-352) and closest_hit (354-394).  Queued on the
+ * context stream; returns once launched.  render_frame is
+ * rdc_reset + rdc_render(0, max_sample_count); render_sample is
+ * rdc_render(sample_count, 1). */
+rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count,
+                      uint32_t max_bounces, uint64_t seed);
+
+/* Copy the float RGBA accumulator (width*height*4 floats, row-major, alpha =
+ * sample count) to host memory.  `count` is the capacity of rgba_out in
+ * floats.  Synchronises the context stream. */
+rdc_status rdc_read_accum(rdc_ctx* ctx, float* rgba_out, size_t count);
+
+/* Overwrite the accumulator from host memory (checkpoint resume) and set the
+ * sample count. */
+rdc_status rdc_write_accum(rdc_ctx* ctx, const float* rgba_in, size_t count,
+                           uint32_t sample_count);
+
+/* Tone-map the accumulator into 8-bit RGBA on the device and copy it to host
+ * memory: CpuRenderer::print_frame_buffer (src/renderer/cpu.rs:221-230),
+ * trunc(clamp(sum / sample_count, 0, 1) * 255).  `count` is the capacity of
+ * rgba_out in bytes.  Synchronises the context stream. */
+rdc_status rdc_read_rgba8(rdc_ctx* ctx, uint32_t sample_count, uint8_t* rgba_out,
+                          size_t count);
+
+/* Counters of the last render (synchronises the context stream). */
+rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out);
+
+/* ---- fixed-input entry points (parity checks of single stages) -------- */
+
+/* Closest hit of n rays against the uploaded scene: Ray::hit / trace_ray /
+ * closest_hit (src/renderer/cpu.rs:23-98, 344-394).  origins and directions
+ * are n*3 floats.  Outputs: t (n), object index (n, -1 on a miss), world
+ * normal after the front-face flip (n*3), front-face flag (n). */
+rdc_status rdc_intersect_rays(rdc_ctx* ctx, const float* origins, const float* directions,
+                              uint32_t n, float* t_out, int32_t* index_out,
+                              float* normal_out, uint8_t* front_out);
+
+/* One scatter step with given random words: the hit branch of per_pixel
+ * (src/renderer/cpu.rs:257-333) for n hits.  Per hit: the ray direction
+ * (3 floats), object index, and 12 raw 32-bit random words (slots 0..10 are
+ * used; their conversion to uniforms is part of the step).  The hit point,
+ * normal and front face are recomputed from the ray origin + t.  Inputs:
+ * origins/directions n*3, t n, index n, words n*12.  Outputs: new origin
+ * n*3, new direction n*3. */
+rdc_status rdc_scatter_fixed(rdc_ctx* ctx, const float* origins, const float* directions,
+                             const float* t, const int32_t* index, const uint32_t* words,
+                             uint32_t n, float* origin_out, float* direction_out);
+
+/* ---- measurement ------------------------------------------------------ */
+
+/* Measure the FP32 issue rate of the context's GPU: every SM runs
+ * independent FFMA chains for a few milliseconds.  Reports FP32 lane
+ * operations per second counting one per lane per clock (SMs x 128 x clock,
+ * the bound of non-contracted FP32 code) and the SM clock that implies.
+ * This is the denominator of the path tracer's roofline; the reference has no
+ * counterpart (it reports wall-clock timers only, src/renderer/timing.rs). */
+rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, double* sm_mhz);
+
+/* ---- host-only helpers (no GPU needed) -------------------------------- */
+
+/* Recompute a camera's view, projection and inverse matrices from its
+ * position/target/up/resolution/projection/clip fields:
+ * Camera::update_matrices (src/scene/camera.rs:210-231). */
+rdc_status rdc_camera_update_matrices(rdc_camera* camera);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAYDAR_CUDA_H */

@@ -1,0 +1,519 @@
+// rdc_api.cpp -- the C ABI of include/raydar_cuda.h: context lifetime, scene
+// validation and flattening, launches, read-back and statistics.
+//
+// Host code only, compiled with -ffp-contract=off: the per-object constants
+// computed here (c.c, r*r, slab bounds, roughness^2, 1/ior, Schlick r0,
+// emission colour * strength) must be the same floats the reference
+// computes inline in src/renderer/cpu.rs.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "raydar_cuda.h"
+#include "rdc_internal.hpp"
+
+using rdc::MatDev;
+
+struct rdc_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+
+    // scene
+    bool has_scene = false;
+    rdc::SceneView view{};
+    float4* d_geom = nullptr;
+    float4* d_hit = nullptr;
+    MatDev* d_mat = nullptr;
+    int4* d_runs = nullptr;
+    size_t cap_obj = 0, cap_runs = 0;
+
+    // frame
+    float4* d_accum = nullptr;
+    uint32_t width = 0, height = 0;
+    uint32_t sample_count = 0;
+    uchar4* d_rgba = nullptr;
+    size_t cap_rgba = 0;
+
+    // counters: [0] work counter (u32 in the low word), [1] segments
+    unsigned long long* d_counters = nullptr;
+
+    // last render
+    uint64_t last_paths = 0;
+    bool last_timed = false;
+    uint32_t last_launches = 0;
+    int render_block = rdc::kRenderBlock;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+rdc_status fail(rdc_ctx* ctx, rdc_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+
+rdc_status cuda_fail(rdc_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return fail(ctx, RDC_ERR_OUT_OF_MEMORY, m);
+    return fail(ctx, RDC_ERR_CUDA, m);
+}
+
+#define RDC_CUDA(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+template <typename T>
+rdc_status ensure(rdc_ctx* ctx, T** ptr, size_t* cap, size_t n, const char* what) {
+    if (n == 0) n = 1;
+    if (*ptr && *cap >= n) return RDC_OK;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)ptr, n * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+    *cap = n;
+    return RDC_OK;
+}
+
+rdc_status set_device(rdc_ctx* ctx) {
+    RDC_CUDA(ctx, cudaSetDevice(ctx->device));
+    return RDC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rdc_version(void) { return "raydar_cuda 0.1.0 (sm_103a)"; }
+
+rdc_status rdc_create(rdc_ctx** out, int device) {
+    g_create_error.clear();
+    if (!out) {
+        g_create_error = "rdc_create: out is NULL";
+        return RDC_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        g_create_error = std::string("rdc_create: no CUDA device ") + std::to_string(device) +
+                         (e != cudaSuccess ? std::string(" (") + cudaGetErrorString(e) + ")" : "");
+        return e != cudaSuccess ? RDC_ERR_CUDA : RDC_ERR_INVALID_ARGUMENT;
+    }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e);
+        return RDC_ERR_CUDA;
+    }
+    if (prop.major * 10 + prop.minor < 100) {
+        g_create_error = std::string("rdc_create: device ") + prop.name +
+                         " is not a Blackwell (sm_10x) GPU; this library is built for sm_103a only";
+        return RDC_ERR_UNSUPPORTED;
+    }
+    rdc_ctx* ctx = new rdc_ctx();
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    auto bail = [&](cudaError_t err, const char* what) {
+        g_create_error = std::string(what) + ": " + cudaGetErrorString(err);
+        rdc_destroy(ctx);
+        return err == cudaErrorMemoryAllocation ? RDC_ERR_OUT_OF_MEMORY : RDC_ERR_CUDA;
+    };
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaMalloc((void**)&ctx->d_counters, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return bail(e, "cudaMalloc(counters)");
+    if ((e = cudaMemset(ctx->d_counters, 0, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return bail(e, "cudaMemset(counters)");
+    *out = ctx;
+    return RDC_OK;
+}
+
+void rdc_destroy(rdc_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->d_geom);
+    cudaFree(ctx->d_hit);
+    cudaFree(ctx->d_mat);
+    cudaFree(ctx->d_runs);
+    cudaFree(ctx->d_accum);
+    cudaFree(ctx->d_rgba);
+    cudaFree(ctx->d_counters);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* rdc_last_error(const rdc_ctx* ctx) {
+    if (!ctx) return g_create_error.c_str();
+    return ctx->err.c_str();
+}
+
+rdc_status rdc_get_stream(rdc_ctx* ctx, void** stream_out) {
+    if (!ctx || !stream_out) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_get_stream: NULL argument");
+    *stream_out = (void*)ctx->stream;
+    return RDC_OK;
+}
+
+rdc_status rdc_synchronize(rdc_ctx* ctx) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RDC_OK;
+}
+
+rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!sc) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: scene is NULL");
+    const rdc_camera& cam = sc->camera;
+    if (cam.resolution_x == 0 || cam.resolution_y == 0)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: zero resolution");
+    if (cam.resolution_x > RDC_MAX_RESOLUTION || cam.resolution_y > RDC_MAX_RESOLUTION)
+        return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: resolution above RDC_MAX_RESOLUTION");
+    if (sc->object_count > RDC_MAX_OBJECTS)
+        return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: object_count " + std::to_string(sc->object_count) +
+                                            " above RDC_MAX_OBJECTS");
+    if (sc->object_count > 0 && !sc->objects)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: objects is NULL");
+    if (sc->world.kind == RDC_WORLD_TRANSPARENT)
+        return fail(ctx, RDC_ERR_UNSUPPORTED,
+                    "rdc_scene_upload: World::Transparent is not supported (todo!() in the reference)");
+    if (sc->world.kind > RDC_WORLD_TRANSPARENT)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: unknown world kind");
+
+    const uint32_t n = sc->object_count;
+    std::vector<float4> geom(2 * (size_t)(n ? n : 1), make_float4(0, 0, 0, 0));
+    std::vector<float4> hit(n ? n : 1, make_float4(0, 0, 0, 0));
+    std::vector<MatDev> mat(n ? n : 1);
+    std::vector<int4> runs;
+    for (uint32_t i = 0; i < n; ++i) {
+        const rdc_object& o = sc->objects[i];
+        if (o.geometry != RDC_GEOMETRY_SPHERE && o.geometry != RDC_GEOMETRY_CUBE)
+            return fail(ctx, RDC_ERR_INVALID_ARGUMENT,
+                        "rdc_scene_upload: object " + std::to_string(i) + " has unknown geometry");
+        const float cx = o.center[0], cy = o.center[1], cz = o.center[2];
+        if (o.geometry == RDC_GEOMETRY_SPHERE) {
+            const float cc = (cx * cx + cy * cy) + cz * cz;
+            geom[2 * i] = make_float4(cx, cy, cz, cc);
+            geom[2 * i + 1] = make_float4(o.radius * o.radius, 0, 0, 0);
+            hit[i] = make_float4(cx, cy, cz, 0.0f);
+        } else {
+            const float h = o.side_length * 0.5f;
+            geom[2 * i] = make_float4(cx - h, cy - h, cz - h, cx + h);
+            geom[2 * i + 1] = make_float4(cy + h, cz + h, 0, 0);
+            hit[i] = make_float4(cx, cy, cz, o.side_length / 2.0f);
+        }
+        const rdc_material& m = o.material;
+        MatDev md;
+        md.a = make_float4(m.albedo[0], m.albedo[1], m.albedo[2], m.roughness * m.roughness);
+        md.b = make_float4(m.emission_color[0] * m.emission_strength, m.emission_color[1] * m.emission_strength,
+                           m.emission_color[2] * m.emission_strength, m.metallic);
+        const float ratio_front = 1.0f / m.ior;
+        const float qf = (ratio_front - 1.0f) / (ratio_front + 1.0f);
+        const float qb = (m.ior - 1.0f) / (m.ior + 1.0f);
+        md.c = make_float4(m.transmission, ratio_front, m.ior, qf * qf);
+        int kind = (int)o.geometry;
+        float kind_bits;
+        std::memcpy(&kind_bits, &kind, 4);
+        md.d = make_float4(qb * qb, kind_bits, 0, 0);
+        mat[i] = md;
+        if (runs.empty() || runs.back().x != kind) runs.push_back(make_int4(kind, (int)i, (int)i + 1, 0));
+        else runs.back().z = (int)i + 1;
+    }
+    if (runs.empty()) runs.push_back(make_int4(0, 0, 0, 0));
+
+    if (rdc_status st = set_device(ctx)) return st;
+    const uint32_t nruns = n ? (uint32_t)runs.size() : 0u;
+    size_t cap_geom = ctx->cap_obj * 2;
+    if (rdc_status st = ensure(ctx, &ctx->d_geom, &cap_geom, geom.size(), "cudaMalloc(geometry)")) return st;
+    size_t cap = ctx->cap_obj;
+    if (rdc_status st = ensure(ctx, &ctx->d_hit, &cap, hit.size(), "cudaMalloc(hit)")) return st;
+    cap = ctx->cap_obj;
+    if (rdc_status st = ensure(ctx, &ctx->d_mat, &cap, mat.size(), "cudaMalloc(materials)")) return st;
+    ctx->cap_obj = cap;
+    if (rdc_status st = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, runs.size(), "cudaMalloc(runs)")) return st;
+    // The previous frame may still read the old scene: order the copies.
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_geom, geom.data(), geom.size() * sizeof(float4),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_hit, hit.data(), hit.size() * sizeof(float4),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_mat, mat.data(), mat.size() * sizeof(MatDev),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_runs, runs.data(), runs.size() * sizeof(int4),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d_bytes += geom.size() * sizeof(float4) + hit.size() * sizeof(float4) + mat.size() * sizeof(MatDev) +
+                      runs.size() * sizeof(int4);
+    // Host staging vectors die at return: wait for the copies.
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+
+    rdc::SceneView& v = ctx->view;
+    v.geom = ctx->d_geom;
+    v.hit = ctx->d_hit;
+    v.mat = ctx->d_mat;
+    v.runs = ctx->d_runs;
+    v.nobj = n;
+    v.nruns = nruns;
+    v.width = cam.resolution_x;
+    v.height = cam.resolution_y;
+    for (int i = 0; i < 3; ++i) v.cam_pos[i] = cam.position[i];
+    for (int i = 0; i < 16; ++i) {
+        v.inv_view[i] = cam.inverse_view_matrix[i];
+        v.inv_proj[i] = cam.inverse_proj_matrix[i];
+    }
+    v.world_kind = sc->world.kind;
+    for (int i = 0; i < 3; ++i) {
+        v.top[i] = sc->world.top_color[i];
+        v.bottom[i] = sc->world.bottom_color[i];
+        v.solid[i] = sc->world.solid_color[i];
+    }
+
+    // Frame buffer follows the resolution (CpuRenderer::frame_buffer, cpu.rs:400-417).
+    if (!ctx->d_accum || ctx->width != cam.resolution_x || ctx->height != cam.resolution_y) {
+        if (ctx->d_accum) cudaFree(ctx->d_accum);
+        ctx->d_accum = nullptr;
+        const size_t npix = (size_t)cam.resolution_x * cam.resolution_y;
+        cudaError_t e = cudaMalloc((void**)&ctx->d_accum, npix * sizeof(float4));
+        if (e != cudaSuccess) {
+            ctx->has_scene = false;
+            return cuda_fail(ctx, e, "cudaMalloc(accumulator)");
+        }
+        RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_accum, 0, npix * sizeof(float4), ctx->stream));
+        ctx->width = cam.resolution_x;
+        ctx->height = cam.resolution_y;
+        ctx->sample_count = 0;
+    }
+    ctx->has_scene = true;
+    return RDC_OK;
+}
+
+rdc_status rdc_reset(rdc_ctx* ctx) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_reset: no scene uploaded");
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_accum, 0, (size_t)ctx->width * ctx->height * sizeof(float4),
+                                  ctx->stream));
+    ctx->sample_count = 0;
+    return RDC_OK;
+}
+
+rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces,
+                      uint64_t seed) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_render: no scene uploaded");
+    if (max_bounces > RDC_MAX_BOUNCES) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: max_bounces above RDC_MAX_BOUNCES");
+    if ((uint64_t)spp_begin + spp_count > 0xFFFFFFFFull)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_render: sample range overflows 32 bits");
+    if (rdc_status st = set_device(ctx)) return st;
+    ctx->last_paths = (uint64_t)ctx->width * ctx->height * spp_count;
+    ctx->last_launches = 0;
+    ctx->last_timed = false;
+    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    if (spp_count == 0) return RDC_OK;
+
+    rdc::RenderParams p;
+    p.sc = ctx->view;
+    p.accum = ctx->d_accum;
+    p.s0 = spp_begin;
+    p.nspp = spp_count;
+    p.max_bounces = max_bounces;
+    p.stream_id = 0;
+    p.key0 = (uint32_t)seed;
+    p.key1 = (uint32_t)(seed >> 32);
+    p.npix = ctx->width * ctx->height;
+    p.work_counter = reinterpret_cast<uint32_t*>(ctx->d_counters);
+    p.segments = ctx->d_counters + 1;
+
+    const size_t smem = rdc::render_smem_bytes(ctx->view.nobj, ctx->view.nruns);
+    int per_sm = 0;
+    RDC_CUDA(ctx, rdc::render_occupancy(ctx->render_block, smem, &per_sm));
+    if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: scene does not fit in shared memory");
+    const uint64_t warps_needed = ((uint64_t)p.npix + 31) / 32;
+    uint64_t grid = (uint64_t)ctx->num_sms * per_sm;
+    const uint64_t grid_needed = (warps_needed * 32 + ctx->render_block - 1) / ctx->render_block;
+    if (grid > grid_needed) grid = grid_needed;
+
+    RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    RDC_CUDA(ctx, rdc::launch_render(p, (int)grid, ctx->render_block, smem, ctx->stream));
+    RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->last_timed = true;
+    ctx->last_launches = 1;
+    ctx->sample_count = spp_begin + spp_count > ctx->sample_count ? spp_begin + spp_count : ctx->sample_count;
+    return RDC_OK;
+}
+
+rdc_status rdc_read_accum(rdc_ctx* ctx, float* rgba_out, size_t count) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_read_accum: no scene uploaded");
+    const size_t need = (size_t)ctx->width * ctx->height * 4;
+    if (!rgba_out || count < need)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_read_accum: output buffer smaller than width*height*4");
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaMemcpyAsync(rgba_out, ctx->d_accum, need * sizeof(float), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->d2h_bytes += need * sizeof(float);
+    return RDC_OK;
+}
+
+rdc_status rdc_write_accum(rdc_ctx* ctx, const float* rgba_in, size_t count, uint32_t sample_count) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_write_accum: no scene uploaded");
+    const size_t need = (size_t)ctx->width * ctx->height * 4;
+    if (!rgba_in || count != need)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_write_accum: input must hold width*height*4 floats");
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_accum, rgba_in, need * sizeof(float), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->h2d_bytes += need * sizeof(float);
+    ctx->sample_count = sample_count;
+    return RDC_OK;
+}
+
+rdc_status rdc_read_rgba8(rdc_ctx* ctx, uint32_t sample_count, uint8_t* rgba_out, size_t count) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_read_rgba8: no scene uploaded");
+    const size_t npix = (size_t)ctx->width * ctx->height;
+    if (!rgba_out || count < npix * 4)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_read_rgba8: output buffer smaller than width*height*4");
+    if (rdc_status st = set_device(ctx)) return st;
+    if (rdc_status st = ensure(ctx, &ctx->d_rgba, &ctx->cap_rgba, npix, "cudaMalloc(rgba8)")) return st;
+    RDC_CUDA(ctx, rdc::launch_tonemap(ctx->d_accum, (uint32_t)npix, sample_count, ctx->d_rgba, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(rgba_out, ctx->d_rgba, npix * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->d2h_bytes += npix * 4;
+    return RDC_OK;
+}
+
+rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out) {
+    if (!ctx || !out) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_stats_get: NULL argument");
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned long long c[2] = {0, 0};
+    RDC_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+    out->segments = c[1];
+    out->paths = ctx->last_paths;
+    out->device_ms = 0.0f;
+    if (ctx->last_timed) RDC_CUDA(ctx, cudaEventElapsedTime(&out->device_ms, ctx->ev0, ctx->ev1));
+    out->sample_count = ctx->sample_count;
+    out->kernel_launches = ctx->last_launches;
+    out->h2d_bytes = ctx->h2d_bytes;
+    out->d2h_bytes = ctx->d2h_bytes;
+    return RDC_OK;
+}
+
+rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, double* sm_mhz) {
+    if (!ctx || !lane_ops_per_second) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_measure_fp32_issue: NULL argument");
+    if (rdc_status st = set_device(ctx)) return st;
+    const int block = 256, blocks_per_sm = 8;  // 64 warps per SM
+    const int grid = ctx->num_sms * blocks_per_sm;
+    float* sink = nullptr;
+    RDC_CUDA(ctx, cudaMalloc((void**)&sink, grid * sizeof(float)));
+    int iters = 256;
+    double best = 0.0;
+    cudaError_t e = cudaSuccess;
+    for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {
+        e = cudaEventRecord(ctx->ev0, ctx->stream);
+        if (e == cudaSuccess) e = rdc::launch_fp32_probe(sink, grid, block, iters, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        if (e != cudaSuccess) break;
+        const double ops = (double)grid * block * iters * 16.0 * rdc::kProbeChains;
+        if (ms > 0.f) best = ops / (ms * 1e-3) > best ? ops / (ms * 1e-3) : best;
+        if (ms < 20.f) iters *= 2;  // grow to a few tens of milliseconds
+    }
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "rdc_measure_fp32_issue");
+    *lane_ops_per_second = best;
+    if (sm_mhz) *sm_mhz = best / (ctx->num_sms * 128.0) / 1e6;
+    ctx->last_timed = false;
+    return RDC_OK;
+}
+
+rdc_status rdc_intersect_rays(rdc_ctx* ctx, const float* origins, const float* directions, uint32_t n,
+                              float* t_out, int32_t* index_out, float* normal_out, uint8_t* front_out) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_intersect_rays: no scene uploaded");
+    if (n == 0) return RDC_OK;
+    if (!origins || !directions || !t_out || !index_out || !normal_out || !front_out)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_intersect_rays: NULL buffer");
+    if (rdc_status st = set_device(ctx)) return st;
+    const size_t f3 = (size_t)n * 3 * sizeof(float);
+    char* buf = nullptr;
+    const size_t total = 3 * f3 + n * sizeof(float) + n * sizeof(int32_t) + n;
+    RDC_CUDA(ctx, cudaMalloc((void**)&buf, total));
+    float* d_o = (float*)buf;
+    float* d_d = (float*)(buf + f3);
+    float* d_n = (float*)(buf + 2 * f3);
+    float* d_t = (float*)(buf + 3 * f3);
+    int32_t* d_i = (int32_t*)(buf + 3 * f3 + n * sizeof(float));
+    uint8_t* d_f = (uint8_t*)(buf + 3 * f3 + n * sizeof(float) + n * sizeof(int32_t));
+    cudaError_t e = cudaMemcpyAsync(d_o, origins, f3, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, directions, f3, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = rdc::launch_intersect_rays(ctx->view, d_o, d_d, n, d_t, d_i, d_n, d_f, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, d_t, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(index_out, d_i, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(normal_out, d_n, f3, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(front_out, d_f, n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "rdc_intersect_rays");
+    return RDC_OK;
+}
+
+rdc_status rdc_scatter_fixed(rdc_ctx* ctx, const float* origins, const float* directions, const float* t,
+                             const int32_t* index, const uint32_t* words, uint32_t n, float* origin_out,
+                             float* direction_out) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_scatter_fixed: no scene uploaded");
+    if (n == 0) return RDC_OK;
+    if (!origins || !directions || !t || !index || !words || !origin_out || !direction_out)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scatter_fixed: NULL buffer");
+    for (uint32_t i = 0; i < n; ++i)
+        if (index[i] < 0 || (uint32_t)index[i] >= ctx->view.nobj)
+            return fail(ctx, RDC_ERR_INVALID_ARGUMENT,
+                        "rdc_scatter_fixed: object index out of range at item " + std::to_string(i));
+    if (rdc_status st = set_device(ctx)) return st;
+    const size_t f3 = (size_t)n * 3 * sizeof(float);
+    const size_t total = 4 * f3 + n * sizeof(float) + n * sizeof(int32_t) + (size_t)n * 12 * sizeof(uint32_t);
+    char* buf = nullptr;
+    RDC_CUDA(ctx, cudaMalloc((void**)&buf, total));
+    float* d_o = (float*)buf;
+    float* d_d = (float*)(buf + f3);
+    float* d_oo = (float*)(buf + 2 * f3);
+    float* d_do = (float*)(buf + 3 * f3);
+    float* d_t = (float*)(buf + 4 * f3);
+    int32_t* d_i = (int32_t*)(buf + 4 * f3 + n * sizeof(float));
+    uint32_t* d_w = (uint32_t*)(buf + 4 * f3 + n * sizeof(float) + n * sizeof(int32_t));
+    cudaError_t e = cudaMemcpyAsync(d_o, origins, f3, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, directions, f3, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t, t, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_i, index, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_w, words, (size_t)n * 12 * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = rdc::launch_scatter_fixed(ctx->view, d_o, d_d, d_t, d_i, d_w, n, d_oo, d_do, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(origin_out, d_oo, f3, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(direction_out, d_do, f3, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "rdc_scatter_fixed");
+    return RDC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+// rdc_internal.hpp -- device data layout and launch parameters shared by the
+// C-ABI layer (rdc_api.cpp) and the kernels (rdc_kernels.cu).
+//
+// Device layout of an uploaded scene (all in HBM, staged per block):
+//   geom[2*i], geom[2*i+1]  per object, scene order (32 B):
+//       sphere: (cx, cy, cz, c.c), (r*r, 0, 0, 0)
+//       cube:   (min.x, min.y, min.z, max.x), (max.y, max.z, 0, 0)
+//   hit[i]   (cx, cy, cz, side/2): what closest_hit needs (16 B)
+//   mat[i]   MatDev, 64 B: everything the scatter step reads for one object
+//   runs[r]  (geometry, begin, end, 0): maximal runs of one geometry kind in
+//            scene order, so the intersection loop visits objects in scene
+//            order (the first-minimum tie rule) with a warp-uniform branch
+//            per run instead of one per object.
+// The per-object constants (c.c, r*r, min/max, roughness^2, 1/ior, Schlick
+// r0, emission colour * strength) are the exact float values the reference
+// computes inline, so hoisting them does not change a single bit.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace rdc {
+
+struct alignas(16) MatDev {
+    float4 a;  // albedo.rgb, roughness^2
+    float4 b;  // emission_color * emission_strength (rgb), metallic
+    float4 c;  // transmission, ratio on a front-face hit (1/ior), ratio on a back-face hit (ior), r0 front
+    float4 d;  // r0 back, geometry kind (int bits), 0, 0
+};
+
+struct SceneView {
+    const float4* geom;
+    const float4* hit;
+    const MatDev* mat;
+    const int4* runs;
+    uint32_t nobj;
+    uint32_t nruns;
+    uint32_t width;
+    uint32_t height;
+    float cam_pos[3];
+    uint32_t world_kind;
+    float inv_view[16];
+    float inv_proj[16];
+    float top[3];
+    float bottom[3];
+    float solid[3];
+};
+
+struct RenderParams {
+    SceneView sc;
+    float4* accum;
+    uint32_t s0;
+    uint32_t nspp;
+    uint32_t max_bounces;
+    uint32_t stream_id;
+    uint32_t key0;
+    uint32_t key1;
+    uint32_t npix;
+    uint32_t* work_counter;
+    unsigned long long* segments;
+};
+
+// Kernel launchers (rdc_kernels.cu).  Each returns the cudaError_t of its
+// launch.
+cudaError_t launch_render(const RenderParams& p, int grid, int block, size_t smem, cudaStream_t s);
+cudaError_t render_occupancy(int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_tonemap(const float4* accum, uint32_t npix, uint32_t sample_count, uchar4* out,
+                           cudaStream_t s);
+cudaError_t launch_intersect_rays(const SceneView& sc, const float* o, const float* d, uint32_t n,
+                                  float* t, int32_t* idx, float* nrm, uint8_t* front,
+                                  cudaStream_t s);
+cudaError_t launch_scatter_fixed(const SceneView& sc, const float* o, const float* d,
+                                 const float* t, const int32_t* idx, const uint32_t* words,
+                                 uint32_t n, float* o_out, float* d_out, cudaStream_t s);
+
+cudaError_t launch_fp32_probe(float* sink, int grid, int block, int iters, cudaStream_t s);
+
+constexpr int kRenderBlock = 256;
+constexpr int kProbeChains = 8;  // independent FFMA chains per thread in the FP32 probe
+
+inline size_t render_smem_bytes(uint32_t nobj, uint32_t nruns) {
+    return (size_t)nobj * 32u + (size_t)nruns * 16u;
+}
+
+}  // namespace rdc

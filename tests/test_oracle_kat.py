@@ -1,0 +1,167 @@
+"""Hand-derived known answers for the CPU oracle (the reference has no tests
+of its own; these pin the restated semantics of src/renderer/cpu.rs)."""
+import numpy as np
+import pytest
+
+import oracle
+from raydar_gb300.scene import Camera, Material, Object, Scene, World
+from raydar_gb300 import scenegen
+
+
+def _scene(objects, w=8, h=4, world=None):
+    cam = Camera.new([0, 0, -5], [0, 0, 0], [0, 1, 0], w, h, 0.01, 1000.0, fov=60.0)
+    return Scene(cam, world or World(), objects)
+
+
+def _sphere(c, r, **m):
+    return Object("Sphere", np.array(c, np.float32), float(r), Material(**m))
+
+
+def _cube(c, s, **m):
+    return Object("Cube", np.array(c, np.float32), float(s), Material(**m))
+
+
+def test_sphere_head_on():
+    sc = _scene([_sphere([0, 0, 5], 1.0)]).to_c()
+    t, idx, n, fr = oracle.intersect(sc, [[0, 0, 0]], [[0, 0, 1]])
+    assert idx[0] == 0 and t[0] == 4.0
+    assert n[0].tolist() == [0.0, 0.0, -1.0] and fr[0] == 1
+
+
+def test_sphere_from_inside_returns_far_root_and_back_face():
+    sc = _scene([_sphere([0, 0, 0], 2.0)]).to_c()
+    t, idx, n, fr = oracle.intersect(sc, [[0, 0, 0]], [[1, 0, 0]])
+    assert idx[0] == 0 and t[0] == 2.0 and fr[0] == 0
+    assert n[0].tolist() == [-1.0, 0.0, 0.0]  # flipped against the ray
+
+
+def test_non_unit_direction_scales_t():
+    sc = _scene([_sphere([0, 0, 5], 1.0)]).to_c()
+    t, idx, _, _ = oracle.intersect(sc, [[0, 0, 0]], [[0, 0, 2]])
+    assert idx[0] == 0 and t[0] == 2.0  # t in units of |d| (cpu.rs:267-271 keeps d unnormalised)
+
+
+def test_sphere_behind_is_missed():
+    sc = _scene([_sphere([0, 0, -5], 1.0)]).to_c()
+    _, idx, _, _ = oracle.intersect(sc, [[0, 0, 0]], [[0, 0, 1]])
+    assert idx[0] == -1
+
+
+def test_cube_slab_and_face_normal():
+    sc = _scene([_cube([0, 0, 0], 2.0)]).to_c()
+    t, idx, n, fr = oracle.intersect(sc, [[0, 5, 0]], [[0, -1, 0]])
+    assert idx[0] == 0 and t[0] == 4.0 and n[0].tolist() == [0.0, 1.0, 0.0] and fr[0] == 1
+    # from inside: exit distance (tmin < 0 -> tmax), back face
+    t, idx, n, fr = oracle.intersect(sc, [[0, 0, 0]], [[0, 0, 1]])
+    assert idx[0] == 0 and t[0] == 1.0 and fr[0] == 0 and n[0].tolist() == [0.0, 0.0, -1.0]
+
+
+def test_cube_axis_parallel_ray_outside_slab_misses():
+    sc = _scene([_cube([0, 0, 0], 2.0)]).to_c()
+    _, idx, _, _ = oracle.intersect(sc, [[0, 3, -5]], [[0, 0, 1]])  # d.y = 0, y outside
+    assert idx[0] == -1
+
+
+def test_first_minimum_wins_on_ties():
+    sc = _scene([_sphere([0, 0, 5], 1.0), _sphere([0, 0, 5], 1.0), _sphere([0, 0, 3], 0.5)]).to_c()
+    t, idx, _, _ = oracle.intersect(sc, [[0, 0, 0]], [[0, 0, 1]])
+    assert idx[0] == 2 and t[0] == 2.5
+    sc = _scene([_sphere([0, 0, 5], 1.0), _sphere([0, 0, 5], 1.0)]).to_c()
+    _, idx, _, _ = oracle.intersect(sc, [[0, 0, 0]], [[0, 0, 1]])
+    assert idx[0] == 0
+
+
+def test_sky_gradient_and_empty_scene_render():
+    sc = _scene([], w=4, h=3).to_c()
+    acc, seg = oracle.render(sc, 0, 3, 5, seed=1)
+    assert seg == 4 * 3 * 3  # one segment (a miss) per path
+    assert np.all(acc[..., 3] == 3.0)
+    top = np.array([0.53, 0.8, 0.92], np.float32)
+    bottom = np.ones(3, np.float32)
+    rgb = acc[..., :3] / 3
+    lo = np.minimum(top, bottom) - 1e-6
+    hi = np.maximum(top, bottom) + 1e-6
+    assert np.all((rgb >= lo) & (rgb <= hi))
+
+
+def test_solid_world_colour():
+    sc = _scene([], w=2, h=2, world=World("SolidColor", color=np.array([0.25, 0.5, 0.75], np.float32))).to_c()
+    acc, _ = oracle.render(sc, 0, 2, 3, seed=0)
+    assert np.all(acc[..., :3] == np.array([0.5, 1.0, 1.5], np.float32))
+
+
+def test_zero_bounces_adds_only_alpha():
+    sc = scenegen.c1_plain(width=6, height=4).scene.to_c()
+    acc, seg = oracle.render(sc, 0, 5, 0, seed=9)
+    assert seg == 0 and np.all(acc[..., :3] == 0) and np.all(acc[..., 3] == 5)
+
+
+def test_emission_is_added_unattenuated():
+    # A camera ray straight into an emissive, black (albedo 0) sphere: light =
+    # emission at the first hit, nothing after (attenuation 0).
+    em = dict(albedo=np.zeros(3, np.float32), emission_color=np.ones(3, np.float32), emission_strength=2.0,
+              roughness=1.0)
+    sc = _scene([_sphere([0, 0, 0], 1.0, **em)], w=1, h=1).to_c()
+    acc, _ = oracle.render(sc, 0, 1, 4, seed=0)
+    # pixel (0,0) sits at the top-left frustum corner, which misses the sphere
+    # for this fov; aim with a 1-pixel camera centred instead:
+    cam = Camera.new([0, 0, -5], [0, 0, 0], [0, 1, 0], 2, 2, 0.01, 1000.0, fov=10.0)
+    s = Scene(cam, World(), [_sphere([0, 0, 0], 3.0, **em)]).to_c()
+    acc, seg = oracle.render(s, 0, 1, 4, seed=0)
+    # pixel (1,1) has uv = (0.5, 0.5): the ray through the centre of the frustum
+    assert acc[1, 1, :3].tolist() == [2.0, 2.0, 2.0]
+
+
+def test_progressive_split_and_threads_are_bit_identical():
+    sc = scenegen.c1_plain(width=24, height=14).scene.to_c()
+    full, s_full = oracle.render(sc, 0, 6, 8, seed=77)
+    a, s1 = oracle.render(sc, 0, 2, 8, seed=77)
+    b, s2 = oracle.render(sc, 2, 4, 8, seed=77, accum=a)
+    assert full.tobytes() == b.tobytes() and s_full == s1 + s2
+    mt, s_mt = oracle.render(sc, 0, 6, 8, seed=77, threads=4)
+    assert mt.tobytes() == full.tobytes() and s_mt == s_full
+
+
+def test_render_pixels_matches_full_render():
+    sc = scenegen.c1_plain(width=20, height=10).scene.to_c()
+    full, _ = oracle.render(sc, 0, 3, 8, seed=5)
+    px = np.array([0, 17, 55, 199], np.uint32)
+    part, _ = oracle.render_pixels(sc, px, 0, 3, 8, seed=5)
+    assert part.tobytes() == full.reshape(-1, 4)[px].tobytes()
+
+
+def test_tonemap_truncates():
+    acc = np.array([[0.5, 1.0, 2.0, 4.0], [-1.0, np.nan, 0.999, 3.9]], np.float32)
+    out = oracle.tonemap(acc, 4)
+    assert out.tolist() == [[31, 63, 127, 255], [0, 0, 63, 248]]
+
+
+def test_mirror_reflection_with_fixed_words():
+    # Metal, roughness 0: the specular lobe is taken (U_metal < 1), direction =
+    # normalize(reflect(d, n)).
+    sc = _scene([_sphere([0, 0, 5], 1.0, metallic=1.0, roughness=0.0)]).to_c()
+    words = np.full((1, 12), 0x12345678, np.uint32)
+    o, d = oracle.scatter(sc, [[0, 0, 0]], [[0, 0, 1]], [4.0], [0], words)
+    assert d[0].tolist() == [0.0, 0.0, -1.0]
+    assert o[0].tolist() == [0.0, 0.0, np.float32(4.0) - np.float32(1e-4)]
+
+
+def test_glass_refracts_straight_through_at_normal_incidence():
+    sc = _scene([_sphere([0, 0, 5], 1.0, transmission=1.0, ior=1.5, roughness=0.0)]).to_c()
+    words = np.zeros((1, 12), np.uint32)
+    words[0, 6] = 0           # U_transmission = 0 < 1: glass branch
+    words[0, 7] = 0xFFFFFFFF  # U_fresnel ~ 1 > r0 = 0.04: refract
+    o, d = oracle.scatter(sc, [[0, 0, 0]], [[0, 0, 1]], [4.0], [0], words)
+    assert d[0].tolist() == [0.0, 0.0, 1.0]
+    assert o[0][2] > 4.0  # offset along the refracted direction
+
+
+def test_diffuse_is_flipped_into_the_hemisphere():
+    sc = _scene([_sphere([0, 0, 5], 1.0, roughness=1.0)]).to_c()
+    rng = np.random.default_rng(3)
+    words = rng.integers(0, 2 ** 32, (256, 12), dtype=np.uint64).astype(np.uint32)
+    words[:, 8] = 0  # U_roughness = 0 < 1: diffuse lobe
+    n = len(words)
+    o, d = oracle.scatter(sc, np.zeros((n, 3)), np.tile([0, 0, 1.0], (n, 1)), np.full(n, 4.0), np.zeros(n),
+                          words)
+    assert np.all(d @ np.array([0, 0, -1.0]) >= 0)
