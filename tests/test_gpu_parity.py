@@ -167,23 +167,29 @@ def test_full_1080p_properties_and_spot_pixels(renderer):
 
 def test_converged_image_matches_independent_oracle_stream(renderer):
     """Statistical parity with independent random streams (the reference's own
-    RNG is unseeded): GPU mean over 32 seeds x 256 spp vs the oracle at 4096
-    spp with another seed, per pixel within 4 sigma, and relative MSE small."""
+    RNG is unseeded, so this is how its converged image is compared): GPU
+    64 seeds x 256 spp vs the oracle 32 other seeds x 512 spp, batch means
+    combined in float64.  Per pixel and channel |difference| within 3 sigma of
+    the batch variance for all but 1% (and none beyond 6 sigma); relative
+    MSE < 1e-4.  The sigma floor 3e-5*|mean| covers float32 running-sum
+    rounding inside one batch, which is all that varies on zero-variance
+    pixels (no pixel jitter: a sky pixel's samples are all equal)."""
     scene = shrink(scenegen.c1_plain().scene, 40, 24)
-    means = []
-    for k in range(32):
+    gpu = []
+    for k in range(64):
         acc, _ = _render_gpu(renderer, scene, 0, 256, 8, seed=1000 + k)
-        means.append(acc[..., :3] / 256)
-    means = np.array(means, np.float64)
-    gm = means.mean(0)
-    sd_batch = means.std(0, ddof=1)
-    ref, _ = oracle.render(scene.to_c(), 0, 4096, 8, 5, threads=16)
-    om = ref[..., :3].astype(np.float64) / 4096
-    sigma = np.sqrt(sd_batch ** 2 / 32 + sd_batch ** 2 * (256 / 4096)) + 1e-6
+        gpu.append(acc[..., :3].astype(np.float64) / 256)
+    cpu = []
+    for k in range(32):
+        acc, _ = oracle.render(scene.to_c(), 0, 512, 8, 5000 + k, threads=16)
+        cpu.append(acc[..., :3].astype(np.float64) / 512)
+    gpu, cpu = np.array(gpu), np.array(cpu)
+    gm, om = gpu.mean(0), cpu.mean(0)
+    sigma = np.sqrt(gpu.var(0, ddof=1) / len(gpu) + cpu.var(0, ddof=1) / len(cpu)) + 3e-5 * np.abs(om) + 1e-7
     z = np.abs(gm - om) / sigma
-    assert (z > 4).mean() < 0.002, float(z.max())
+    assert (z > 3).mean() < 0.01 and z.max() < 6, float(z.max())
     rel_mse = ((gm - om) ** 2).mean() / (om ** 2).mean()
-    assert rel_mse < 1e-3, rel_mse
+    assert rel_mse < 1e-4, rel_mse
 
 
 def test_scene_errors(renderer):
