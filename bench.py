@@ -206,14 +206,15 @@ def run_reference(args):
 
 
 # -------------------------------------------------------------------- ours --
-def _traffic_per_segment():
-    """DRAM bytes per segment of the render kernel from the committed ncu summary."""
+def _traffic_per_launch():
+    """DRAM bytes of one 1080p render launch from the committed ncu summary
+    (per pixel, independent of spp)."""
     f = ROOT / "profiles" / "render_kernel_traffic.json"
     if not f.exists():
         return None
     try:
         d = json.loads(f.read_text())
-        return float(d["dram_bytes_per_segment"])
+        return float(d["dram_bytes_per_launch"])
     except (ValueError, KeyError):
         return None
 
@@ -257,6 +258,8 @@ def run_ours(args):
 
     seed_base = 1000 + 100000 * rank
     for i in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
         render(seed_base + 50000 + i)
     r._check(lib.rdc_synchronize(ctx), "sync")
 
@@ -345,7 +348,7 @@ def run_ours(args):
     seg_per_launch = my_segments / len(segs)
     achieved = ops * seg_per_launch / mean_kernel_s / 1e12
     peak = ops_s.value / 1e12
-    tps = _traffic_per_segment()
+    traffic = _traffic_per_launch()
     line = {
         "metric": METRIC, "value": total_segments / elapsed, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
@@ -358,7 +361,7 @@ def run_ours(args):
         "roofline": {
             "bound": "fp32", "kernel": "render_kernel", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak if peak > 0 else None,
-            "traffic": (tps * seg_per_launch if tps is not None else None),
+            "traffic": traffic,
             "ops_per_segment": ops,
             "peak_source": f"measured in this run: FFMA issue rate {peak:.2f} T lane-ops/s "
                            f"(= {mhz.value:.0f} MHz x SMs x 128), one op per lane per clock",
