@@ -178,6 +178,31 @@ rdc_status rdc_reset(rdc_ctx* ctx);
 rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count,
                       uint32_t max_bounces, uint64_t seed);
 
+/* Render without allocating any GPU memory.  For callers that cannot call
+ * cudaMalloc -- an application whose device memory belongs to another
+ * allocator (a game engine, a Vulkan or OpenGL interop layer), a real-time
+ * loop that forbids allocation after start-up, a plugin with a fixed memory
+ * budget.  It does what rdc_scene_upload + rdc_render do on a context, but
+ * the caller passes `accum_device`, a device pointer to its own
+ * width*height*4-float RGBA accumulator (added to in sample order, exactly as
+ * rdc_render adds), and the scene is copied into a fixed-size device array
+ * inside the library (RDC_STATIC_SCRATCH_BYTES, held by every GPU that loads
+ * the library until exit) together with the counters the kernel works from.
+ * Limits: at most RDC_STATIC_MAX_OBJECTS objects (RDC_ERR_LIMIT above).
+ * Work is queued on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * of the calling thread's current device.  The first call on a device looks
+ * up the array's device address; make it before any stream capture.  Every
+ * call on a device shares the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  If `segments_out` is non-NULL the call
+ * waits for the render and stores its segment count.  A message for a
+ * non-OK status is written to `error_out` (capacity bytes, may be NULL).
+ * No counterpart in the reference: it has no allocation-free entry point. */
+#define RDC_STATIC_MAX_OBJECTS 1024u
+#define RDC_STATIC_SCRATCH_BYTES 131328u /* 256 B counters + 128 B per object slot */
+rdc_status rdc_render_static(const rdc_scene_desc* scene, float* accum_device, uint32_t spp_begin,
+                             uint32_t spp_count, uint32_t max_bounces, uint64_t seed, void* stream,
+                             uint64_t* segments_out, char* error_out, size_t error_capacity);
+
 /* Copy the float RGBA accumulator (width*height*4 floats, row-major, alpha =
  * sample count) to host memory.  `count` is the capacity of rgba_out in
  * floats.  Synchronises the context stream. */

@@ -92,6 +92,8 @@ SIGNATURES = {
     "rdc_scene_upload": (C.c_int, [_P, C.POINTER(RdcSceneDesc)]),
     "rdc_reset": (C.c_int, [_P]),
     "rdc_render": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
+    "rdc_render_static": (C.c_int, [C.POINTER(RdcSceneDesc), C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                    C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64), C.c_char_p, C.c_size_t]),
     "rdc_read_accum": (C.c_int, [_P, _FP, C.c_size_t]),
     "rdc_write_accum": (C.c_int, [_P, _FP, C.c_size_t, C.c_uint32]),
     "rdc_read_rgba8": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint8), C.c_size_t]),
