@@ -12,9 +12,13 @@
 #include <vector>
 
 #include "raydar_cuda.h"
+#include "rdc_flatten.hpp"
 #include "rdc_internal.hpp"
 
 using rdc::MatDev;
+
+// Shared memory a block may use for the staged scene (records + runs).
+constexpr size_t kMaxSceneSmem = 200 * 1024;
 
 struct rdc_ctx {
     int device = 0;
@@ -26,11 +30,11 @@ struct rdc_ctx {
     // scene
     bool has_scene = false;
     rdc::SceneView view{};
-    float4* d_geom = nullptr;
+    float4* d_rec = nullptr;
     float4* d_hit = nullptr;
     MatDev* d_mat = nullptr;
     int4* d_runs = nullptr;
-    size_t cap_obj = 0, cap_runs = 0;
+    size_t cap_obj = 0, cap_runs = 0, cap_rec = 0;
 
     // frame
     float4* d_accum = nullptr;
@@ -145,7 +149,7 @@ void rdc_destroy(rdc_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    cudaFree(ctx->d_geom);
+    cudaFree(ctx->d_rec);
     cudaFree(ctx->d_hit);
     cudaFree(ctx->d_mat);
     cudaFree(ctx->d_runs);
@@ -196,50 +200,21 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
         return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: unknown world kind");
 
     const uint32_t n = sc->object_count;
-    std::vector<float4> geom(2 * (size_t)(n ? n : 1), make_float4(0, 0, 0, 0));
-    std::vector<float4> hit(n ? n : 1, make_float4(0, 0, 0, 0));
-    std::vector<MatDev> mat(n ? n : 1);
-    std::vector<int4> runs;
-    for (uint32_t i = 0; i < n; ++i) {
-        const rdc_object& o = sc->objects[i];
-        if (o.geometry != RDC_GEOMETRY_SPHERE && o.geometry != RDC_GEOMETRY_CUBE)
+    for (uint32_t i = 0; i < n; ++i)
+        if (sc->objects[i].geometry != RDC_GEOMETRY_SPHERE && sc->objects[i].geometry != RDC_GEOMETRY_CUBE)
             return fail(ctx, RDC_ERR_INVALID_ARGUMENT,
                         "rdc_scene_upload: object " + std::to_string(i) + " has unknown geometry");
-        const float cx = o.center[0], cy = o.center[1], cz = o.center[2];
-        if (o.geometry == RDC_GEOMETRY_SPHERE) {
-            const float cc = (cx * cx + cy * cy) + cz * cz;
-            geom[2 * i] = make_float4(cx, cy, cz, cc);
-            geom[2 * i + 1] = make_float4(o.radius * o.radius, 0, 0, 0);
-            hit[i] = make_float4(cx, cy, cz, 0.0f);
-        } else {
-            const float h = o.side_length * 0.5f;
-            geom[2 * i] = make_float4(cx - h, cy - h, cz - h, cx + h);
-            geom[2 * i + 1] = make_float4(cy + h, cz + h, 0, 0);
-            hit[i] = make_float4(cx, cy, cz, o.side_length / 2.0f);
-        }
-        const rdc_material& m = o.material;
-        MatDev md;
-        md.a = make_float4(m.albedo[0], m.albedo[1], m.albedo[2], m.roughness * m.roughness);
-        md.b = make_float4(m.emission_color[0] * m.emission_strength, m.emission_color[1] * m.emission_strength,
-                           m.emission_color[2] * m.emission_strength, m.metallic);
-        const float ratio_front = 1.0f / m.ior;
-        const float qf = (ratio_front - 1.0f) / (ratio_front + 1.0f);
-        const float qb = (m.ior - 1.0f) / (m.ior + 1.0f);
-        md.c = make_float4(m.transmission, ratio_front, m.ior, qf * qf);
-        int kind = (int)o.geometry;
-        float kind_bits;
-        std::memcpy(&kind_bits, &kind, 4);
-        md.d = make_float4(qb * qb, kind_bits, 0, 0);
-        mat[i] = md;
-        if (runs.empty() || runs.back().x != kind) runs.push_back(make_int4(kind, (int)i, (int)i + 1, 0));
-        else runs.back().z = (int)i + 1;
-    }
-    if (runs.empty()) runs.push_back(make_int4(0, 0, 0, 0));
+    const rdc::FlatCounts fc = rdc::flat_counts(sc);
+    if (rdc::render_smem_bytes(fc.nrec, fc.nruns) > kMaxSceneSmem)
+        return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: scene records exceed the shared-memory budget");
+    std::vector<float4> rec(fc.nrec ? fc.nrec : 1, make_float4(0, 0, 0, 0));
+    std::vector<float4> hit(n ? n : 1, make_float4(0, 0, 0, 0));
+    std::vector<MatDev> mat(n ? n : 1);
+    std::vector<int4> runs(fc.nruns ? fc.nruns : 1, make_int4(0, 0, 0, 0));
+    const bool fast_div = rdc::flatten(sc, rec.data(), hit.data(), mat.data(), runs.data());
 
     if (rdc_status st = set_device(ctx)) return st;
-    const uint32_t nruns = n ? (uint32_t)runs.size() : 0u;
-    size_t cap_geom = ctx->cap_obj * 2;
-    if (rdc_status st = ensure(ctx, &ctx->d_geom, &cap_geom, geom.size(), "cudaMalloc(geometry)")) return st;
+    if (rdc_status st = ensure(ctx, &ctx->d_rec, &ctx->cap_rec, rec.size(), "cudaMalloc(records)")) return st;
     size_t cap = ctx->cap_obj;
     if (rdc_status st = ensure(ctx, &ctx->d_hit, &cap, hit.size(), "cudaMalloc(hit)")) return st;
     cap = ctx->cap_obj;
@@ -247,7 +222,7 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     ctx->cap_obj = cap;
     if (rdc_status st = ensure(ctx, &ctx->d_runs, &ctx->cap_runs, runs.size(), "cudaMalloc(runs)")) return st;
     // The previous frame may still read the old scene: order the copies.
-    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_geom, geom.data(), geom.size() * sizeof(float4),
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * sizeof(float4),
                                   cudaMemcpyHostToDevice, ctx->stream));
     RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_hit, hit.data(), hit.size() * sizeof(float4),
                                   cudaMemcpyHostToDevice, ctx->stream));
@@ -255,18 +230,21 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
                                   cudaMemcpyHostToDevice, ctx->stream));
     RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_runs, runs.data(), runs.size() * sizeof(int4),
                                   cudaMemcpyHostToDevice, ctx->stream));
-    ctx->h2d_bytes += geom.size() * sizeof(float4) + hit.size() * sizeof(float4) + mat.size() * sizeof(MatDev) +
+    ctx->h2d_bytes += rec.size() * sizeof(float4) + hit.size() * sizeof(float4) + mat.size() * sizeof(MatDev) +
                       runs.size() * sizeof(int4);
     // Host staging vectors die at return: wait for the copies.
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
     rdc::SceneView& v = ctx->view;
-    v.geom = ctx->d_geom;
+    v.rec = ctx->d_rec;
+    v.nrec = fc.nrec;
     v.hit = ctx->d_hit;
     v.mat = ctx->d_mat;
     v.runs = ctx->d_runs;
     v.nobj = n;
-    v.nruns = nruns;
+    v.nruns = fc.nruns;
+    v.fast_div = fast_div ? 1u : 0u;
+    v.neg_zero = make_float2(-0.0f, -0.0f);
     v.width = cam.resolution_x;
     v.height = cam.resolution_y;
     for (int i = 0; i < 3; ++i) v.cam_pos[i] = cam.position[i];
@@ -337,7 +315,7 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
     p.work_counter = reinterpret_cast<uint32_t*>(ctx->d_counters);
     p.segments = ctx->d_counters + 1;
 
-    const size_t smem = rdc::render_smem_bytes(ctx->view.nobj, ctx->view.nruns);
+    const size_t smem = rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
     int per_sm = 0;
     RDC_CUDA(ctx, rdc::render_occupancy(ctx->render_block, smem, &per_sm));
     if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: scene does not fit in shared memory");

@@ -67,69 +67,213 @@ __device__ __forceinline__ V3 vsub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y,
 __device__ __forceinline__ V3 vmul(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
 __device__ __forceinline__ V3 vneg(V3 a) { return V3{-a.x, -a.y, -a.z}; }
 __device__ __forceinline__ float vdot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+// cgmath normalize: v * RN(1 / RN(sqrt(v.v))); __frcp_rn is the IEEE quotient 1/x.
 __device__ __forceinline__ V3 vnormalize(V3 a) {
-    const float inv = 1.0f / sqrtf(vdot(a, a));
+    const float inv = __frcp_rn(__fsqrt_rn(vdot(a, a)));
     return vmul(a, inv);
 }
 __device__ __forceinline__ float rsignum(float a) { return a != a ? a : copysignf(1.0f, a); }
 
 // --------------------------------------------------------- intersection ---
+// Division.  The reference divides with IEEE round-to-nearest (`/` in Rust).
+// Along one ray every slab test divides by the same three direction
+// components and every sphere test by the same d.d, so the kernels divide by
+// multiplying with a per-ray correctly rounded reciprocal y = RN(1/b) and
+// applying Markstein's final correction step (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990): q0 = RN(a*y) is a faithful quotient, the residual
+// a - b*q0 is exact in an FMA, and RN(q0 + residual*y) is exactly RN(a/b) --
+// the IEEE quotient, bit for bit -- as long as a, b, the quotient and the
+// residual stay clear of overflow and the subnormal range.  The guards below
+// (per ray: direction components in [2^-40, 16], origin components 0 or in
+// [2^-60, 2^60], d.d in [2^-34, 2^10]; per scene: cube sides > 0 and slab
+// bounds 0 or in [2^-60, 2^60]; per sphere hit: numerator in [2^-60, 2^60])
+// keep every operand there; a ray outside them takes IEEE division.
+__device__ __forceinline__ float div_recip(float a, float b, float y) {
+    const float q0 = __fmul_rn(a, y);
+    const float r = __fmaf_rn(-q0, b, a);
+    return __fmaf_rn(r, y, q0);
+}
+
+__device__ __forceinline__ bool in_range(float v, float lo, float hi) {
+    const float m = fabsf(v);
+    return m >= lo && m <= hi;
+}
+
+// Two-wide float arithmetic (Blackwell's packed FP32x2 instructions).  Each
+// component is rounded exactly like the scalar instruction, so pairing two
+// spheres, or the two slab planes of one axis, changes no bit; it halves the
+// issue slots the FP32 work takes in this issue-bound loop.
+//
+// Contraction: ptxas fuses a packed multiply into a following packed add
+// (one rounding instead of the reference's two) even for .rn instructions
+// under -fmad=false, and folds fma(a, b, -0) + c the same way.  A packed
+// product is therefore computed as fma.rn(a, b, z) with z = (-0, -0) taken
+// from a kernel parameter: RN(a*b + -0) is exactly RN(a*b) for every input
+// (a zero product keeps its sign), and ptxas cannot prove z is zero, so the
+// product is rounded on its own as the reference rounds it.
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+#define RDC_F32X2_BINARY(name, op)                                                           \
+    __device__ __forceinline__ float2 name(float2 a, float2 b) {                               \
+        float2 d;                                                                              \
+        asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" \
+            op " rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"                                  \
+            : "=f"(d.x), "=f"(d.y)                                                             \
+            : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                         \
+        return d;                                                                              \
+    }
+RDC_F32X2_BINARY(add2, "add.rn.f32x2")
+RDC_F32X2_BINARY(sub2, "sub.rn.f32x2")  // a - b (IEEE: a + (-b))
+#undef RDC_F32X2_BINARY
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// RN(a*b) per component; nz must be the (-0, -0) kernel parameter.
+__device__ __forceinline__ float2 mul2(float2 a, float2 b, float2 nz) { return fma2(a, b, nz); }
+
+// Two quotients by one divisor b (reciprocal y = RN(1/b), nb = -b): the
+// Markstein step above on both components.
+__device__ __forceinline__ float2 div2_recip(float2 a, float2 nb, float2 y, float2 nz) {
+    const float2 q0 = mul2(a, y, nz);
+    const float2 r = fma2(q0, nb, a);
+    return fma2(r, y, q0);
+}
+
 // Per-ray values every primitive test reuses (the same floats the reference
-// recomputes inside each test).
+// recomputes inside each test) and the reciprocals of the divisors.
 struct RayPre {
     V3 o, d;
     float a;   // d.d
     float od;  // o.d
     float oo;  // o.o
+    float ra;  // RN(1/a)
+    V3 rd;     // RN(1/d) per component
+    bool fast; // operands inside the exact-reciprocal-division range
+    float2 nz; // (-0, -0), opaque to the compiler (see mul2)
 };
 
-__device__ __forceinline__ RayPre ray_pre(V3 o, V3 d) {
+__device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float2 nz) {
     RayPre r;
+    r.nz = nz;
     r.o = o;
     r.d = d;
     r.a = vdot(d, d);
     r.od = vdot(o, d);
     r.oo = vdot(o, o);
+    r.ra = __frcp_rn(r.a);
+    r.rd = mk(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+    const float D0 = 9.094947e-13f /* 2^-40 */, D1 = 16.0f;
+    const float O0 = 8.6736174e-19f /* 2^-60 */, O1 = 1.1529215e18f /* 2^60 */;
+    r.fast = in_range(d.x, D0, D1) && in_range(d.y, D0, D1) && in_range(d.z, D0, D1) &&
+             (o.x == 0.0f || in_range(o.x, O0, O1)) && (o.y == 0.0f || in_range(o.y, O0, O1)) &&
+             (o.z == 0.0f || in_range(o.z, O0, O1)) && in_range(r.a, 5.820766e-11f /* 2^-34 */, 1024.0f);
     return r;
 }
 
-// hit_sphere, src/renderer/cpu.rs:34-62, then the first-minimum update of
-// trace_ray (cpu.rs:345-349): replace only on a strictly smaller t.
-__device__ __forceinline__ void sphere_test(const RayPre& r, float4 g0, float rr, int i,
-                                            float& best, int& bidx) {
-    const float dc = (r.d.x * g0.x + r.d.y * g0.y) + r.d.z * g0.z;
+template <bool Fast>
+__device__ __forceinline__ float sphere_div(float num, const RayPre& r) {
+    if (Fast) {
+        if (in_range(num, 8.6736174e-19f, 1.1529215e18f)) return div_recip(num, r.a, r.ra);
+    }
+    return num / r.a;
+}
+
+// hit_sphere (src/renderer/cpu.rs:34-62), pass 1: the discriminant of up to
+// 32 spheres of a run (packed pairs, rdc_flatten.hpp), two per instruction,
+// into a bit mask of the spheres that can return a hit.  disc < 0 returns
+// None in the reference.  With the fast (guarded) arithmetic a sphere whose
+// whole line intersection lies behind the origin is dropped too: k >= 2^-63
+// (k*k normal) and disc < k*k*(1 - 2^-20) force RN(sqrt(disc)) < k, so both
+// roots are negative and the reference returns None.
+template <bool Fast>
+__device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__ pr, int n,
+                                                      const RayPre& r) {
+    const float2 dx = f2(r.d.x, r.d.x), dy = f2(r.d.y, r.d.y), dz = f2(r.d.z, r.d.z);
+    const float2 ox = f2(r.o.x, r.o.x), oy = f2(r.o.y, r.o.y), oz = f2(r.o.z, r.o.z);
+    const float2 od = f2(r.od, r.od), oo = f2(r.oo, r.oo), a = f2(r.a, r.a);
+    const float CULL = 0.99999905f;  // 1 - 2^-20
+    uint32_t m = 0, bit = 1u;
+    const int np = (n + 1) >> 1;
+#pragma unroll 4
+    for (int p = 0; p < np; ++p) {
+        const float4 A = pr[3 * p];
+        const float4 B = pr[3 * p + 1];
+        const float2 rr = *reinterpret_cast<const float2*>(&pr[3 * p + 2]);
+        const float2 cx = f2(A.x, A.y), cy = f2(A.z, A.w), cz = f2(B.x, B.y), cc = f2(B.z, B.w);
+        const float2 dc = add2(add2(mul2(dx, cx, r.nz), mul2(dy, cy, r.nz)), mul2(dz, cz, r.nz));
+        const float2 k = sub2(od, dc);
+        const float2 oc = add2(add2(mul2(ox, cx, r.nz), mul2(oy, cy, r.nz)), mul2(oz, cz, r.nz));
+        const float2 c = sub2(add2(sub2(oo, add2(oc, oc)), cc), rr);
+        const float2 kk = mul2(k, k, r.nz);
+        const float2 disc = sub2(kk, mul2(a, c, r.nz));
+        bool g0 = disc.x >= 0.0f, g1 = disc.y >= 0.0f;
+        if (Fast) {
+            const float2 lim = mul2(kk, f2(CULL, CULL), r.nz);
+            g0 = g0 && !(k.x >= 1.0842022e-19f /* 2^-63 */ && disc.x < lim.x);
+            g1 = g1 && !(k.y >= 1.0842022e-19f && disc.y < lim.y);
+        }
+        m |= (g0 ? bit : 0u) | (g1 ? (bit << 1) : 0u);
+        bit <<= 2;
+    }
+    return n >= 32 ? m : (m & ((1u << n) - 1u));
+}
+
+// hit_sphere pass 2 for one candidate (run-relative index j of the chunk's
+// records), then the first-minimum update of trace_ray (cpu.rs:345-349):
+// replace only on a strictly smaller t.  Candidates are visited in scene
+// order, so the tie rule is the reference's.
+template <bool Fast>
+__device__ __forceinline__ void sphere_exact(const float4* __restrict__ pr, int j, int obj,
+                                             const RayPre& r, float& best, int& bidx) {
+    const float* q = reinterpret_cast<const float*>(pr + 3 * (j >> 1)) + (j & 1);
+    const float cx = q[0], cy = q[2], cz = q[4], cc = q[6], rr = q[8];
+    const float dc = (r.d.x * cx + r.d.y * cy) + r.d.z * cz;
     const float k = r.od - dc;
-    const float oc = (r.o.x * g0.x + r.o.y * g0.y) + r.o.z * g0.z;
-    const float c = ((r.oo - 2.0f * oc) + g0.w) - rr;
+    const float oc = (r.o.x * cx + r.o.y * cy) + r.o.z * cz;
+    const float c = ((r.oo - 2.0f * oc) + cc) - rr;
     const float disc = k * k - r.a * c;
-    if (disc >= 0.0f) {
-        const float sq = sqrtf(disc);
-        const float t1 = (-k - sq) / r.a;
-        float t = t1;
-        bool ok = t1 >= 0.0f;
-        if (!ok) {
-            const float t2 = (-k + sq) / r.a;
-            t = t2;
-            ok = t2 >= 0.0f;
-        }
-        if (ok && (bidx < 0 || t < best)) {
-            best = t;
-            bidx = i;
-        }
+    const float sq = __fsqrt_rn(disc);
+    const float t1 = sphere_div<Fast>(-k - sq, r);
+    float t = t1;
+    bool ok = t1 >= 0.0f;
+    if (!ok) {
+        const float t2 = sphere_div<Fast>(-k + sq, r);
+        t = t2;
+        ok = t2 >= 0.0f;
+    }
+    if (ok && (bidx < 0 || t < best)) {
+        best = t;
+        bidx = obj;
     }
 }
 
-// hit_cube, src/renderer/cpu.rs:64-98 (true division per axis).
-__device__ __forceinline__ void cube_test(const RayPre& r, float4 g0, float4 g1, int i,
+// hit_cube, src/renderer/cpu.rs:64-98: the two slab planes of each axis
+// divided as a pair.
+template <bool Fast>
+__device__ __forceinline__ void cube_test(const float4* __restrict__ cr, int i, const RayPre& r,
                                           float& best, int& bidx) {
-    const float tx1 = (g0.x - r.o.x) / r.d.x;
-    const float tx2 = (g0.w - r.o.x) / r.d.x;
-    const float ty1 = (g0.y - r.o.y) / r.d.y;
-    const float ty2 = (g1.x - r.o.y) / r.d.y;
-    const float tz1 = (g0.z - r.o.z) / r.d.z;
-    const float tz2 = (g1.y - r.o.z) / r.d.z;
-    const float tmin = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
-    const float tmax = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
+    const float4 A = cr[0];
+    const float2 Z = *reinterpret_cast<const float2*>(&cr[1]);
+    const float2 ax = sub2(f2(A.x, A.y), f2(r.o.x, r.o.x));
+    const float2 ay = sub2(f2(A.z, A.w), f2(r.o.y, r.o.y));
+    const float2 az = sub2(Z, f2(r.o.z, r.o.z));
+    float2 tx, ty, tz;
+    if (Fast) {
+        tx = div2_recip(ax, f2(-r.d.x, -r.d.x), f2(r.rd.x, r.rd.x), r.nz);
+        ty = div2_recip(ay, f2(-r.d.y, -r.d.y), f2(r.rd.y, r.rd.y), r.nz);
+        tz = div2_recip(az, f2(-r.d.z, -r.d.z), f2(r.rd.z, r.rd.z), r.nz);
+    } else {
+        tx = f2(ax.x / r.d.x, ax.y / r.d.x);
+        ty = f2(ay.x / r.d.y, ay.y / r.d.y);
+        tz = f2(az.x / r.d.z, az.y / r.d.z);
+    }
+    const float tmin = fmaxf(fmaxf(fminf(tx.x, tx.y), fminf(ty.x, ty.y)), fminf(tz.x, tz.y));
+    const float tmax = fminf(fminf(fmaxf(tx.x, tx.y), fmaxf(ty.x, ty.y)), fmaxf(tz.x, tz.y));
     if (!(tmax < 0.0f) && !(tmin > tmax)) {
         const float t = tmin < 0.0f ? tmax : tmin;
         if (bidx < 0 || t < best) {
@@ -140,29 +284,43 @@ __device__ __forceinline__ void cube_test(const RayPre& r, float4 g0, float4 g1,
 }
 
 // Brute-force closest hit over all objects in scene order.
-__device__ __forceinline__ void intersect_all(const float4* __restrict__ geom,
-                                              const int4* __restrict__ runs, int nruns,
-                                              const RayPre& r, float& best, int& bidx) {
+template <bool Fast>
+__device__ __forceinline__ void intersect_runs(const float4* __restrict__ rec,
+                                               const int4* __restrict__ runs, int nruns,
+                                               const RayPre& r, float& best, int& bidx) {
     best = __int_as_float(0x7f800000);
     bidx = -1;
     for (int q = 0; q < nruns; ++q) {
         const int4 run = runs[q];
         if (run.x == 0) {
-#pragma unroll 4
-            for (int i = run.y; i < run.z; ++i) {
-                const float4 g0 = geom[2 * i];
-                const float rr = geom[2 * i + 1].x;
-                sphere_test(r, g0, rr, i, best, bidx);
+            for (int cb = run.y; cb < run.z; cb += 32) {
+                const int n = min(32, run.z - cb);
+                const float4* pr = rec + run.w + 3 * ((cb - run.y) >> 1);
+                uint32_t m = sphere_candidates<Fast>(pr, n, r);
+                while (m != 0u) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1u;
+                    sphere_exact<Fast>(pr, j, cb + j, r, best, bidx);
+                }
             }
         } else {
+            const float4* cr = rec + run.w;
 #pragma unroll 2
-            for (int i = run.y; i < run.z; ++i) {
-                const float4 g0 = geom[2 * i];
-                const float4 g1 = geom[2 * i + 1];
-                cube_test(r, g0, g1, i, best, bidx);
-            }
+            for (int i = run.y; i < run.z; ++i) cube_test<Fast>(cr + 2 * (i - run.y), i, r, best, bidx);
         }
     }
+}
+
+// `scene_fast`: every slab bound of the scene is inside the exact-division
+// range (computed on upload).
+__device__ __forceinline__ void intersect_all(const float4* __restrict__ rec,
+                                              const int4* __restrict__ runs, int nruns,
+                                              bool scene_fast, const RayPre& r, float& best,
+                                              int& bidx) {
+    if (scene_fast && r.fast)
+        intersect_runs<true>(rec, runs, nruns, r, best, bidx);
+    else
+        intersect_runs<false>(rec, runs, nruns, r, best, bidx);
 }
 
 struct HitRec {

@@ -1,21 +1,22 @@
 // rdc_internal.hpp -- device data layout and launch parameters shared by the
 // C-ABI layer (rdc_api.cpp) and the kernels (rdc_kernels.cu).
 //
-// Device layout of an uploaded scene (all in HBM, staged per block):
-//   geom[2*i], geom[2*i+1]  per object, scene order (32 B):
-//       sphere: (cx, cy, cz, c.c), (r*r, 0, 0, 0)
-//       cube:   (min.x, min.y, min.z, max.x), (max.y, max.z, 0, 0)
+// Device layout of an uploaded scene (all in HBM; rec and runs are staged in
+// shared memory per block):
+//   rec[]    intersection records (rdc_flatten.hpp): spheres in packed pairs
+//            (48 B per pair), cubes as (min, max) pairs per axis (32 B)
 //   hit[i]   (cx, cy, cz, side/2): what closest_hit needs (16 B)
 //   mat[i]   MatDev, 64 B: everything the scatter step reads for one object
-//   runs[r]  (geometry, begin, end, 0): maximal runs of one geometry kind in
-//            scene order, so the intersection loop visits objects in scene
-//            order (the first-minimum tie rule) with a warp-uniform branch
-//            per run instead of one per object.
+//   runs[r]  (geometry, begin, end, first record): maximal runs of one
+//            geometry kind in scene order, so the intersection loop visits
+//            objects in scene order (the first-minimum tie rule) with a
+//            warp-uniform branch per run instead of one per object.
 // The per-object constants (c.c, r*r, min/max, roughness^2, 1/ior, Schlick
 // r0, emission colour * strength) are the exact float values the reference
 // computes inline, so hoisting them does not change a single bit.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -30,12 +31,15 @@ struct alignas(16) MatDev {
 };
 
 struct SceneView {
-    const float4* geom;
+    const float4* rec;  // intersection records (rdc_flatten.hpp), staged in shared memory
+    uint32_t nrec;      // float4 records
     const float4* hit;
     const MatDev* mat;
     const int4* runs;
     uint32_t nobj;
     uint32_t nruns;
+    uint32_t fast_div;  // every cube passes cube_fast_div_ok (exact reciprocal division allowed)
+    float2 neg_zero;    // (-0, -0): the addend of packed products (rdc_device.cuh, mul2)
     uint32_t width;
     uint32_t height;
     float cam_pos[3];
@@ -76,11 +80,23 @@ cudaError_t launch_scatter_fixed(const SceneView& sc, const float* o, const floa
 
 cudaError_t launch_fp32_probe(float* sink, int grid, int block, int iters, cudaStream_t s);
 
+// A cube whose slab bounds keep the kernels' exact reciprocal division in
+// range (rdc_device.cuh): positive finite side, every bound 0 or with
+// magnitude in [2^-60, 2^60].
+inline bool slab_bound_ok(float b) {
+    const float m = std::fabs(b);
+    return b == 0.0f || (m >= 0x1p-60f && m <= 0x1p60f);
+}
+inline bool cube_fast_div_ok(float side, const float4& g0, const float4& g1) {
+    return side > 0.0f && std::isfinite(side) && slab_bound_ok(g0.x) && slab_bound_ok(g0.y) &&
+           slab_bound_ok(g0.z) && slab_bound_ok(g0.w) && slab_bound_ok(g1.x) && slab_bound_ok(g1.y);
+}
+
 constexpr int kRenderBlock = 256;
 constexpr int kProbeChains = 8;  // independent FFMA chains per thread in the FP32 probe
 
-inline size_t render_smem_bytes(uint32_t nobj, uint32_t nruns) {
-    return (size_t)nobj * 32u + (size_t)nruns * 16u;
+inline size_t render_smem_bytes(uint32_t nrec, uint32_t nruns) {
+    return (size_t)nrec * 16u + (size_t)nruns * 16u;
 }
 
 }  // namespace rdc

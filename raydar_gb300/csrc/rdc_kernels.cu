@@ -18,11 +18,11 @@
 
 namespace rdc {
 
-__global__ void __launch_bounds__(kRenderBlock) render_kernel(const RenderParams P) {
+__global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderParams P) {
     extern __shared__ float4 smem[];
-    float4* s_geom = smem;
-    int4* s_runs = reinterpret_cast<int4*>(smem + 2 * P.sc.nobj);
-    for (uint32_t i = threadIdx.x; i < 2 * P.sc.nobj; i += blockDim.x) s_geom[i] = P.sc.geom[i];
+    float4* s_rec = smem;
+    int4* s_runs = reinterpret_cast<int4*>(smem + P.sc.nrec);
+    for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
     for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
     __syncthreads();
 
@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kRenderBlock) render_kernel(const RenderParams
 
     int pix = -1;
     uint32_t sample = 0, send = 0, bounce = 0;
-    V3 po = mk(0.f, 0.f, 0.f), pd = po, o = po, d = po, atten = po, light = po;
+    V3 o = mk(0.f, 0.f, 0.f), d = o, atten = o, light = o;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t segs = 0;
     bool pool_open = true;
@@ -52,12 +52,10 @@ __global__ void __launch_bounds__(kRenderBlock) render_kernel(const RenderParams
                 if (mine < P.npix) {
                     pix = (int)mine;
                     acc = P.accum[pix];
-                    primary_ray(P.sc, mine % P.sc.width, mine / P.sc.width, po, pd);
+                    primary_ray(P.sc, mine % P.sc.width, mine / P.sc.width, o, d);
                     sample = P.s0;
                     send = P.s0 + P.nspp;
                     bounce = 0;
-                    o = po;
-                    d = pd;
                     atten = mk(1.f, 1.f, 1.f);
                     light = mk(0.f, 0.f, 0.f);
                 }
@@ -69,10 +67,10 @@ __global__ void __launch_bounds__(kRenderBlock) render_kernel(const RenderParams
         bool done;
         if (bounce < P.max_bounces) {
             ++segs;
-            const RayPre r = ray_pre(o, d);
+            const RayPre r = ray_pre(o, d, P.sc.neg_zero);
             float t;
             int idx;
-            intersect_all(s_geom, s_runs, nruns, r, t, idx);
+            intersect_all(s_rec, s_runs, nruns, P.sc.fast_div != 0u, r, t, idx);
             if (idx >= 0) {
                 const float4 hi = __ldg(&P.sc.hit[idx]);
                 const MatDev m = P.sc.mat[idx];
@@ -111,8 +109,9 @@ __global__ void __launch_bounds__(kRenderBlock) render_kernel(const RenderParams
                 P.accum[pix] = acc;
                 pix = -1;
             } else {
-                o = po;
-                d = pd;
+                // Next sample of the same pixel: the primary ray is recomputed
+                // (identical every sample) rather than kept in registers.
+                primary_ray(P.sc, (uint32_t)pix % P.sc.width, (uint32_t)pix / P.sc.width, o, d);
                 atten = mk(1.f, 1.f, 1.f);
                 light = mk(0.f, 0.f, 0.f);
                 bounce = 0;
@@ -147,10 +146,10 @@ __global__ void intersect_rays_kernel(const SceneView sc, const float* __restric
     if (i >= n) return;
     const V3 ro = mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
     const V3 rd = mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
-    const RayPre r = ray_pre(ro, rd);
+    const RayPre r = ray_pre(ro, rd, sc.neg_zero);
     float t;
     int idx;
-    intersect_all(sc.geom, sc.runs, (int)sc.nruns, r, t, idx);
+    intersect_all(sc.rec, sc.runs, (int)sc.nruns, sc.fast_div != 0u, r, t, idx);
     idx_out[i] = idx;
     if (idx >= 0) {
         const MatDev m = sc.mat[idx];

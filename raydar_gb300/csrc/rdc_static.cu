@@ -22,22 +22,23 @@
 #include <mutex>
 
 #include "raydar_cuda.h"
+#include "rdc_flatten.hpp"
 #include "rdc_internal.hpp"
 
 namespace {
 
 constexpr size_t kCounterBytes = 256;
-constexpr size_t kGeomBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 32;
+constexpr size_t kRecBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 32;  // <= 2 float4 per object
 constexpr size_t kHitBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 16;
 constexpr size_t kMatBytes = (size_t)RDC_STATIC_MAX_OBJECTS * sizeof(rdc::MatDev);
 constexpr size_t kRunBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 16;
-constexpr size_t kGeomOff = kCounterBytes;
-constexpr size_t kHitOff = kGeomOff + kGeomBytes;
+constexpr size_t kRecOff = kCounterBytes;
+constexpr size_t kHitOff = kRecOff + kRecBytes;
 constexpr size_t kMatOff = kHitOff + kHitBytes;
 constexpr size_t kRunOff = kMatOff + kMatBytes;
 constexpr size_t kScratchBytes = kRunOff + kRunBytes;
 static_assert(kScratchBytes == RDC_STATIC_SCRATCH_BYTES, "scratch layout and header disagree");
-static_assert(kGeomOff % 256 == 0 && kHitOff % 256 == 0 && kMatOff % 256 == 0 && kRunOff % 256 == 0,
+static_assert(kRecOff % 256 == 0 && kHitOff % 256 == 0 && kMatOff % 256 == 0 && kRunOff % 256 == 0,
               "scratch regions must stay 256-byte aligned");
 
 // The scratch.  Its name in host code is only a stand-in for the symbol, not
@@ -78,32 +79,13 @@ rdc_status setup(int device, unsigned char** scratch, int* sms, char* err, size_
     return RDC_OK;
 }
 
-// Per-object constants, the same floats rdc_scene_upload computes.
-void flatten_object(const rdc_object& o, float4* geom2, float4* hit, rdc::MatDev* mat) {
-    const float cx = o.center[0], cy = o.center[1], cz = o.center[2];
-    if (o.geometry == RDC_GEOMETRY_SPHERE) {
-        geom2[0] = make_float4(cx, cy, cz, (cx * cx + cy * cy) + cz * cz);
-        geom2[1] = make_float4(o.radius * o.radius, 0, 0, 0);
-        *hit = make_float4(cx, cy, cz, 0.0f);
-    } else {
-        const float h = o.side_length * 0.5f;
-        geom2[0] = make_float4(cx - h, cy - h, cz - h, cx + h);
-        geom2[1] = make_float4(cy + h, cz + h, 0, 0);
-        *hit = make_float4(cx, cy, cz, o.side_length / 2.0f);
-    }
-    const rdc_material& m = o.material;
-    mat->a = make_float4(m.albedo[0], m.albedo[1], m.albedo[2], m.roughness * m.roughness);
-    mat->b = make_float4(m.emission_color[0] * m.emission_strength, m.emission_color[1] * m.emission_strength,
-                         m.emission_color[2] * m.emission_strength, m.metallic);
-    const float ratio_front = 1.0f / m.ior;
-    const float qf = (ratio_front - 1.0f) / (ratio_front + 1.0f);
-    const float qb = (m.ior - 1.0f) / (m.ior + 1.0f);
-    mat->c = make_float4(m.transmission, ratio_front, m.ior, qf * qf);
-    int kind = (int)o.geometry;
-    float kind_bits;
-    std::memcpy(&kind_bits, &kind, 4);
-    mat->d = make_float4(qb * qb, kind_bits, 0, 0);
-}
+// Host staging for the flattened scene: static storage (no allocation),
+// guarded by a mutex while a call flattens and copies it.
+std::mutex g_stage_mutex;
+float4 g_stage_rec[2 * RDC_STATIC_MAX_OBJECTS];
+float4 g_stage_hit[RDC_STATIC_MAX_OBJECTS];
+rdc::MatDev g_stage_mat[RDC_STATIC_MAX_OBJECTS];
+int4 g_stage_runs[RDC_STATIC_MAX_OBJECTS];
 
 }  // namespace
 
@@ -173,57 +155,27 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
     if (rdc_status st = setup(device, &scratch, &sms, error_out, error_capacity)) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-    float4* d_geom = reinterpret_cast<float4*>(scratch + kGeomOff);
+    float4* d_rec = reinterpret_cast<float4*>(scratch + kRecOff);
     float4* d_hit = reinterpret_cast<float4*>(scratch + kHitOff);
     rdc::MatDev* d_mat = reinterpret_cast<rdc::MatDev*>(scratch + kMatOff);
     int4* d_runs = reinterpret_cast<int4*>(scratch + kRunOff);
     unsigned long long* d_counters = reinterpret_cast<unsigned long long*>(scratch);
 
-    // Flatten the scene in fixed chunks on the stack and copy each chunk into
-    // the scratch (pageable copies are staged before cudaMemcpyAsync returns).
-    constexpr uint32_t kChunk = 32;
-    float4 cg[2 * kChunk];
-    float4 ch[kChunk];
-    rdc::MatDev cm[kChunk];
-    int4 cr[kChunk];
-    uint32_t nruns = 0, runs_flushed = 0, run_fill = 0;
-    int4 cur = make_int4(-1, 0, 0, 0);
+    // Flatten into the static host staging area and copy it into the scratch
+    // (pageable copies are staged before cudaMemcpyAsync returns).
     const uint32_t n = sc->object_count;
-    for (uint32_t base = 0; base < n; base += kChunk) {
-        const uint32_t cnt = n - base < kChunk ? n - base : kChunk;
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const rdc_object& o = sc->objects[base + j];
-            flatten_object(o, &cg[2 * j], &ch[j], &cm[j]);
-            const int kind = (int)o.geometry;
-            if (cur.x == kind) {
-                cur.z = (int)(base + j) + 1;
-            } else {
-                if (cur.x >= 0) {
-                    cr[run_fill++] = cur;
-                    ++nruns;
-                    if (run_fill == kChunk) {
-                        e = cudaMemcpyAsync(d_runs + runs_flushed, cr, kChunk * sizeof(int4), cudaMemcpyHostToDevice, s);
-                        if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemcpyAsync(runs)");
-                        runs_flushed += kChunk;
-                        run_fill = 0;
-                    }
-                }
-                cur = make_int4(kind, (int)(base + j), (int)(base + j) + 1, 0);
-            }
-        }
-        e = cudaMemcpyAsync(d_geom + 2 * base, cg, 2 * cnt * sizeof(float4), cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_hit + base, ch, cnt * sizeof(float4), cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_mat + base, cm, cnt * sizeof(rdc::MatDev), cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemcpyAsync(scene)");
+    const rdc::FlatCounts fc = rdc::flat_counts(sc);
+    bool fast_div = true;
+    {
+        std::lock_guard<std::mutex> lock(g_stage_mutex);
+        fast_div = rdc::flatten(sc, g_stage_rec, g_stage_hit, g_stage_mat, g_stage_runs);
+        if (fc.nrec) e = cudaMemcpyAsync(d_rec, g_stage_rec, fc.nrec * sizeof(float4), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(d_hit, g_stage_hit, n * sizeof(float4), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(d_mat, g_stage_mat, n * sizeof(rdc::MatDev), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && fc.nruns)
+            e = cudaMemcpyAsync(d_runs, g_stage_runs, fc.nruns * sizeof(int4), cudaMemcpyHostToDevice, s);
     }
-    if (cur.x >= 0) {
-        cr[run_fill++] = cur;
-        ++nruns;
-    }
-    if (run_fill > 0) {
-        e = cudaMemcpyAsync(d_runs + runs_flushed, cr, run_fill * sizeof(int4), cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemcpyAsync(runs)");
-    }
+    if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemcpyAsync(scene)");
     // The work counter and the segment counter must start at zero.
     e = cudaMemsetAsync(d_counters, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemsetAsync(counters)");
@@ -231,12 +183,15 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
     if (spp_count > 0) {
         rdc::RenderParams p;
         rdc::SceneView& v = p.sc;
-        v.geom = d_geom;
+        v.rec = d_rec;
+        v.nrec = fc.nrec;
         v.hit = d_hit;
         v.mat = d_mat;
         v.runs = d_runs;
         v.nobj = n;
-        v.nruns = nruns;
+        v.nruns = fc.nruns;
+        v.fast_div = fast_div ? 1u : 0u;
+        v.neg_zero = make_float2(-0.0f, -0.0f);
         v.width = cam.resolution_x;
         v.height = cam.resolution_y;
         for (int i = 0; i < 3; ++i) v.cam_pos[i] = cam.position[i];
@@ -261,7 +216,7 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
         p.work_counter = reinterpret_cast<uint32_t*>(d_counters);
         p.segments = d_counters + 1;
 
-        const size_t smem = rdc::render_smem_bytes(n, nruns);
+        const size_t smem = rdc::render_smem_bytes(fc.nrec, fc.nruns);
         int per_sm = 0;
         e = rdc::render_occupancy(rdc::kRenderBlock, smem, &per_sm);
         if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "render occupancy");

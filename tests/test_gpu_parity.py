@@ -119,6 +119,30 @@ def test_fixed_ray_batch_intersection_matches_oracle(renderer, name):
     assert bits_equal(t, rt) and bits_equal(nrm, rn) and np.array_equal(fr, rf)
 
 
+def test_borderline_rays_match_oracle(renderer, golden_dir):
+    """Rays on which one ulp decides the hit, taken from renders of the
+    reference's benchmark scene: a primary ray tangent to sphere 24
+    (discriminant exactly 0) and a ray leaving sphere 8 whose c term cancels to
+    -8e-7.  A packed multiply fused into the following add (one rounding
+    instead of two) drops both hits; the kernels must match the oracle here."""
+    scene = shrink(Scene.load(golden_dir / "benchmark.rscn"), 80, 45)
+    renderer.upload(scene)
+    o = np.array([[-10.082242965698242, 4.5850090980529785, -10.082204818725586],
+                  [-0.2938964068889618, 0.652721107006073, -3.8709042072296143]], np.float32)
+    d = np.array([[0.907118022441864, -0.2591124475002289, 0.3316586911678314],
+                  [-0.6680339574813843, -0.1301172971725464, 0.7326664924621582]], np.float32)
+    n = len(o)
+    t = np.zeros(n, np.float32)
+    idx = np.zeros(n, np.int32)
+    nrm = np.zeros((n, 3), np.float32)
+    fr = np.zeros(n, np.uint8)
+    assert renderer.lib.rdc_intersect_rays(renderer.ctx, native.fptr(o), native.fptr(d), n, native.fptr(t),
+                                           native.iptr(idx), native.fptr(nrm), native.u8ptr(fr)) == 0
+    rt, ridx, rn, rf = oracle.intersect(scene.to_c(), o, d)
+    assert ridx.tolist() == [24, 8]
+    assert np.array_equal(idx, ridx) and bits_equal(t, rt) and bits_equal(nrm, rn)
+
+
 def test_fixed_uniform_scatter_matches_oracle(renderer):
     scene = SCENES["c2_96x54"]()
     renderer.upload(scene)
