@@ -86,9 +86,12 @@ __device__ __forceinline__ float rsignum(float a) { return a != a ? a : copysign
 // the IEEE quotient, bit for bit -- as long as a, b, the quotient and the
 // residual stay clear of overflow and the subnormal range.  The guards below
 // (per ray: direction components in [2^-40, 16], origin components 0 or in
-// [2^-60, 2^60], d.d in [2^-34, 2^10]; per scene: cube sides > 0 and slab
-// bounds 0 or in [2^-60, 2^60]; per sphere hit: numerator in [2^-60, 2^60])
-// keep every operand there; a ray outside them takes IEEE division.
+// [2^-60, 2^50], d.d in [2^-34, 2^10]; per scene: cube sides > 0 and slab
+// bounds 0 or in [2^-60, 2^60], sphere centres and radii finite and at most
+// 2^50; per sphere hit: numerator in [2^-60, 2^60])
+// keep every operand there; a ray outside them takes IEEE division.  The
+// same guards (with origins and sphere centres and radii at most 2^50) keep
+// every value of the sphere candidate pass finite.
 __device__ __forceinline__ float div_recip(float a, float b, float y) {
     const float q0 = __fmul_rn(a, y);
     const float r = __fmaf_rn(-q0, b, a);
@@ -168,7 +171,7 @@ __device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float2 nz) {
     r.ra = __frcp_rn(r.a);
     r.rd = mk(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
     const float D0 = 9.094947e-13f /* 2^-40 */, D1 = 16.0f;
-    const float O0 = 8.6736174e-19f /* 2^-60 */, O1 = 1.1529215e18f /* 2^60 */;
+    const float O0 = 8.6736174e-19f /* 2^-60 */, O1 = 1.1258999e15f /* 2^50 */;
     r.fast = in_range(d.x, D0, D1) && in_range(d.y, D0, D1) && in_range(d.z, D0, D1) &&
              (o.x == 0.0f || in_range(o.x, O0, O1)) && (o.y == 0.0f || in_range(o.y, O0, O1)) &&
              (o.z == 0.0f || in_range(o.z, O0, O1)) && in_range(r.a, 5.820766e-11f /* 2^-34 */, 1024.0f);
@@ -196,8 +199,13 @@ __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__
     const float2 dx = f2(r.d.x, r.d.x), dy = f2(r.d.y, r.d.y), dz = f2(r.d.z, r.d.z);
     const float2 ox = f2(r.o.x, r.o.x), oy = f2(r.o.y, r.o.y), oz = f2(r.o.z, r.o.z);
     const float2 od = f2(r.od, r.od), oo = f2(r.oo, r.oo), a = f2(r.a, r.a);
-    const float CULL = 0.99999905f;  // 1 - 2^-20
-    uint32_t m = 0, bit = 1u;
+    const float CULL = 0.99999905f;                     // 1 - 2^-20
+    const float2 ntiny = f2(-1.0842022e-19f, -1.0842022e-19f);  // -2^-63
+    // Each sphere's decision is the sign bit of a word (clear = candidate),
+    // shifted into the mask with one funnel shift: sphere j of the chunk ends
+    // at bit n-1-j.  disc is never -0 (k*k >= +0), so sign(disc) is exactly
+    // `disc < 0`; NaN signs only ever add candidates, which pass 2 rejects.
+    uint32_t m = 0;
     const int np = (n + 1) >> 1;
 #pragma unroll 4
     for (int p = 0; p < np; ++p) {
@@ -211,16 +219,25 @@ __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__
         const float2 c = sub2(add2(sub2(oo, add2(oc, oc)), cc), rr);
         const float2 kk = mul2(k, k, r.nz);
         const float2 disc = sub2(kk, mul2(a, c, r.nz));
-        bool g0 = disc.x >= 0.0f, g1 = disc.y >= 0.0f;
+        uint32_t w0, w1;
         if (Fast) {
+            // cull (k >= 2^-63 and disc < lim) from the signs of k - 2^-63 and
+            // disc - lim, both exact in sign (finite operands: range guards).
             const float2 lim = mul2(kk, f2(CULL, CULL), r.nz);
-            g0 = g0 && !(k.x >= 1.0842022e-19f /* 2^-63 */ && disc.x < lim.x);
-            g1 = g1 && !(k.y >= 1.0842022e-19f && disc.y < lim.y);
+            const float2 kd = add2(k, ntiny);
+            const float2 ld = sub2(disc, lim);
+            // keep = ~s_disc & (s_kd | ~s_ld): bit 31 clear <=> candidate
+            w0 = ~(~__float_as_uint(disc.x) & (__float_as_uint(kd.x) | ~__float_as_uint(ld.x)));
+            w1 = ~(~__float_as_uint(disc.y) & (__float_as_uint(kd.y) | ~__float_as_uint(ld.y)));
+        } else {
+            w0 = __float_as_uint(disc.x);
+            w1 = __float_as_uint(disc.y);
         }
-        m |= (g0 ? bit : 0u) | (g1 ? (bit << 1) : 0u);
-        bit <<= 2;
+        m = __funnelshift_l(~w0, m, 1);
+        m = __funnelshift_l(~w1, m, 1);
     }
-    return n >= 32 ? m : (m & ((1u << n) - 1u));
+    if (2 * np > n) m >>= 1;  // drop the padding half of an odd chunk
+    return m;
 }
 
 // hit_sphere pass 2 for one candidate (run-relative index j of the chunk's
@@ -297,9 +314,10 @@ __device__ __forceinline__ void intersect_runs(const float4* __restrict__ rec,
                 const int n = min(32, run.z - cb);
                 const float4* pr = rec + run.w + 3 * ((cb - run.y) >> 1);
                 uint32_t m = sphere_candidates<Fast>(pr, n, r);
-                while (m != 0u) {
-                    const int j = __ffs(m) - 1;
-                    m &= m - 1u;
+                while (m != 0u) {  // highest bit first = scene order
+                    const int pos = 31 - __clz(m);
+                    m ^= 1u << pos;
+                    const int j = n - 1 - pos;
                     sphere_exact<Fast>(pr, j, cb + j, r, best, bidx);
                 }
             }

@@ -66,8 +66,8 @@ inline MatDev flat_material(const rdc_object& o) {
     return md;
 }
 
-// Fill the arrays sized by flat_counts; returns whether every cube allows the
-// kernels' exact reciprocal division (cube_fast_div_ok).
+// Fill the arrays sized by flat_counts; returns whether every object allows
+// the kernels' guarded fast path (cube_fast_div_ok, sphere_fast_ok).
 inline bool flatten(const rdc_scene_desc* sc, float4* rec, float4* hit, MatDev* mat, int4* runs) {
     const uint32_t n = sc->object_count;
     bool fast_div = true;
@@ -88,6 +88,7 @@ inline bool flatten(const rdc_scene_desc* sc, float4* rec, float4* hit, MatDev* 
                 rec[off++] = make_float4(c1[0], c2[0], c1[1], c2[1]);
                 rec[off++] = make_float4(c1[2], c2[2], cc1, cc2);
                 rec[off++] = make_float4(s1.radius * s1.radius, s2.radius * s2.radius, 0.0f, 0.0f);
+                fast_div = fast_div && sphere_fast_ok(s1.center, s1.radius) && sphere_fast_ok(s2.center, s2.radius);
             }
         } else {
             for (uint32_t p = i; p < j; ++p) {

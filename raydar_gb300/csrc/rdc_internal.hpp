@@ -38,7 +38,7 @@ struct SceneView {
     const int4* runs;
     uint32_t nobj;
     uint32_t nruns;
-    uint32_t fast_div;  // every cube passes cube_fast_div_ok (exact reciprocal division allowed)
+    uint32_t fast_div;  // every object passes cube_fast_div_ok / sphere_fast_ok (guarded fast path allowed)
     float2 neg_zero;    // (-0, -0): the addend of packed products (rdc_device.cuh, mul2)
     uint32_t width;
     uint32_t height;
@@ -90,6 +90,13 @@ inline bool slab_bound_ok(float b) {
 inline bool cube_fast_div_ok(float side, const float4& g0, const float4& g1) {
     return side > 0.0f && std::isfinite(side) && slab_bound_ok(g0.x) && slab_bound_ok(g0.y) &&
            slab_bound_ok(g0.z) && slab_bound_ok(g0.w) && slab_bound_ok(g1.x) && slab_bound_ok(g1.y);
+}
+
+// A sphere whose centre and radius keep the candidate pass finite
+// (rdc_device.cuh): finite, magnitudes at most 2^50.
+inline bool sphere_fast_ok(const float c[3], float radius) {
+    return std::fabs(c[0]) <= 0x1p50f && std::fabs(c[1]) <= 0x1p50f && std::fabs(c[2]) <= 0x1p50f &&
+           std::fabs(radius) <= 0x1p50f;
 }
 
 constexpr int kRenderBlock = 256;
