@@ -55,6 +55,9 @@ def _args():
     p.add_argument("--spp", type=int, default=0, help="samples per pixel per step (default: the workload's 1024)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched (config 3) measurement")
+    p.add_argument("--batch-only", action="store_true", help="only the batched (config 3) measurement")
+    p.add_argument("--batch-spp-div", type=int, default=1, help="divide every batch item's spp (small profiling case)")
     return p.parse_args()
 
 
@@ -219,6 +222,64 @@ def _traffic_per_launch():
         return None
 
 
+def batch_bench(local: int, steps: int, spp_div: int = 1):
+    """Config 3: the 64 seeded scenes of c3_batch in one persistent launch (CUDA
+    graph, launch shape from the autotuner) vs one render launch per scene
+    (each scene resident in its own context, launched back to back)."""
+    from raydar_gb300 import CudaRenderer, RendererConfig, scenegen
+    from raydar_gb300.batch import BatchRenderer
+
+    ws = scenegen.c3_batch()
+    items = [(w.scene, max(1, w.spp // spp_div), w.max_bounces, 3000 + i) for i, w in enumerate(ws)]
+    br = BatchRenderer(items, device=local)
+    tune = br.autotune()
+    br.render()
+    br.stats()
+    segs, dev_ms = 0, 0.0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        br.render()
+        st = br.stats()  # synchronises
+        segs += st.segments
+        dev_ms += st.device_ms
+    batch_s = (time.perf_counter() - t0) / steps
+    paths = br.stats().paths
+    br.close()
+
+    rs = []
+    for sc, spp, b, seed in items:
+        r = CudaRenderer(RendererConfig(max_sample_count=spp, max_bounces=b), device=local, seed=seed)
+        r.upload(sc)
+        rs.append(r)
+    for r, (sc, spp, b, seed) in zip(rs, items):  # warm-up
+        r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+        r.render_range(0, spp)
+        r.stats()
+    ps_segs = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for r, (sc, spp, b, seed) in zip(rs, items):
+            r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+            r.render_range(0, spp)
+            ps_segs += r.stats().segments  # synchronises: one scene at a time
+    per_scene_s = (time.perf_counter() - t0) / steps
+    for r in rs:
+        r.close()
+    n = len(items)
+    return {
+        "workload": f"c3_batch: {n} scenes, width 128..1024, 16:9 or 1:1, spp 16..512 log-uniform, "
+                    f"4..12 bounces, 4..200 spheres + 0..20 cubes; {paths / 1e9:.2f} G paths per batch",
+        "scenes_per_s": n / batch_s,
+        "segments_per_s": segs / steps / batch_s,
+        "kernel_ms_per_batch": dev_ms / steps,
+        "per_scene_scenes_per_s": n / per_scene_s,
+        "per_scene_segments_per_s": ps_segs / steps / per_scene_s,
+        "speedup_vs_per_scene": per_scene_s / batch_s,
+        "launch_config": {k: tune[k] for k in ("block_size", "blocks_per_sm", "refill_min_idle")},
+        "steps": steps,
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -333,6 +394,10 @@ def run_ours(args):
     else:
         e2e_total = float(e2e_segs)
 
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = batch_bench(local, max(1, min(args.steps, 3)), args.batch_spp_div)
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -378,12 +443,18 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": base,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
 
 
 def main():
     args = _args()
+    if args.batch_only:
+        import torch
+        torch.cuda.set_device(_dist()[2])
+        print(json.dumps({"batched": batch_bench(_dist()[2], max(1, min(args.steps, 3)), args.batch_spp_div)}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

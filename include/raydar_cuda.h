@@ -223,6 +223,47 @@ rdc_status rdc_read_rgba8(rdc_ctx* ctx, uint32_t sample_count, uint8_t* rgba_out
 /* Counters of the last render (synchronises the context stream). */
 rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out);
 
+/* ---- batched rendering: many scenes in one persistent launch ---------- */
+
+/* One scene of a batch: samples [0, spp) of every pixel, at most max_bounces
+ * segments per path, RNG key `seed` and RNG stream = the item's index. */
+typedef struct rdc_batch_item {
+    const rdc_scene_desc* scene;
+    uint32_t spp;
+    uint32_t max_bounces;
+    uint64_t seed;
+} rdc_batch_item;
+
+/* Launch shape of the persistent kernels. */
+typedef struct rdc_launch_config {
+    uint32_t block_size;      /* threads per block: 64, 128 or 256 */
+    uint32_t blocks_per_sm;   /* resident blocks per SM, i.e. paths in flight per SM; 0 = as many as fit */
+    uint32_t refill_min_idle; /* idle lanes of a warp before it takes new pixels (1..32) */
+} rdc_launch_config;
+
+/* Copy `count` scenes to the device as one batch (replacing any previous
+ * batch of the context), allocate one accumulator per scene, and capture the
+ * batch's launch (clear + persistent kernel) in a CUDA graph.  The reference
+ * renders one scene per process run (src/main.rs:10-24); a batch is N such
+ * render_frame calls (src/renderer/cpu.rs:119-133) fused into one launch. */
+rdc_status rdc_batch_upload(rdc_ctx* ctx, const rdc_batch_item* items, uint32_t count);
+
+/* Render every scene of the batch from cleared accumulators: one graph
+ * launch on the context stream (returns once launched). */
+rdc_status rdc_batch_render(rdc_ctx* ctx);
+
+/* Copy scene `index`'s accumulator (its width*height*4 floats) to host memory. */
+rdc_status rdc_batch_read_accum(rdc_ctx* ctx, uint32_t index, float* rgba_out, size_t count);
+
+/* Set / get the batch launch shape (re-captures the graph). */
+rdc_status rdc_batch_set_config(rdc_ctx* ctx, const rdc_launch_config* config);
+rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config);
+
+/* Time the batch under a grid of launch shapes (block size x blocks per SM x
+ * refill threshold), keep the fastest and return it with its device time.
+ * Leaves the accumulators of the last trial; render again for results. */
+rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* best_ms_out);
+
 /* ---- fixed-input entry points (parity checks of single stages) -------- */
 
 /* Closest hit of n rays against the uploaded scene: Ray::hit / trace_ray /

@@ -5,6 +5,7 @@
 // computed here (c.c, r*r, slab bounds, roughness^2, 1/ior, Schlick r0,
 // emission colour * strength) must be the same floats the reference
 // computes inline in src/renderer/cpu.rs.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -52,6 +53,26 @@ struct rdc_ctx {
     uint32_t last_launches = 0;
     int render_block = rdc::kRenderBlock;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
+
+    // batch (rdc_batch_upload)
+    struct Batch {
+        uint32_t n = 0;
+        rdc::BatchScene* d_scenes = nullptr;
+        float4* d_rec = nullptr;
+        float4* d_hit = nullptr;
+        MatDev* d_mat = nullptr;
+        int4* d_runs = nullptr;
+        float4* d_accum = nullptr;
+        uint32_t* d_pixel_counters = nullptr;
+        std::vector<size_t> accum_off;  // in float4
+        std::vector<uint32_t> width, height;
+        size_t accum_total = 0;         // float4
+        size_t smem = 0;                // dynamic shared memory: the largest scene's records + runs
+        uint64_t paths = 0;
+        rdc_launch_config cfg{256, 0, 1};
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    } batch;
 };
 
 namespace {
@@ -92,6 +113,60 @@ rdc_status set_device(rdc_ctx* ctx) {
     RDC_CUDA(ctx, cudaSetDevice(ctx->device));
     return RDC_OK;
 }
+
+// Checks shared by every scene entry point.  The reference accepts any
+// numbers (a NaN sphere is simply never hit); what it cannot render -- the
+// Transparent world, a todo!() panic -- is reported instead of panicking.
+rdc_status check_scene(rdc_ctx* ctx, const rdc_scene_desc* sc, const std::string& who) {
+    if (!sc) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, who + ": scene is NULL");
+    const rdc_camera& cam = sc->camera;
+    if (cam.resolution_x == 0 || cam.resolution_y == 0)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, who + ": zero resolution");
+    if (cam.resolution_x > RDC_MAX_RESOLUTION || cam.resolution_y > RDC_MAX_RESOLUTION)
+        return fail(ctx, RDC_ERR_LIMIT, who + ": resolution above RDC_MAX_RESOLUTION");
+    if (sc->object_count > RDC_MAX_OBJECTS)
+        return fail(ctx, RDC_ERR_LIMIT,
+                    who + ": object_count " + std::to_string(sc->object_count) + " above RDC_MAX_OBJECTS");
+    if (sc->object_count > 0 && !sc->objects) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, who + ": objects is NULL");
+    if (sc->world.kind == RDC_WORLD_TRANSPARENT)
+        return fail(ctx, RDC_ERR_UNSUPPORTED,
+                    who + ": World::Transparent is not supported (todo!() in the reference)");
+    if (sc->world.kind > RDC_WORLD_TRANSPARENT) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, who + ": unknown world kind");
+    for (uint32_t i = 0; i < sc->object_count; ++i)
+        if (sc->objects[i].geometry != RDC_GEOMETRY_SPHERE && sc->objects[i].geometry != RDC_GEOMETRY_CUBE)
+            return fail(ctx, RDC_ERR_INVALID_ARGUMENT, who + ": object " + std::to_string(i) + " has unknown geometry");
+    return RDC_OK;
+}
+
+void fill_view(rdc::SceneView& v, const rdc_scene_desc* sc, const float4* rec, uint32_t nrec, const float4* hit,
+               const MatDev* mat, const int4* runs, uint32_t nruns, bool fast_div) {
+    const rdc_camera& cam = sc->camera;
+    v.rec = rec;
+    v.nrec = nrec;
+    v.hit = hit;
+    v.mat = mat;
+    v.runs = runs;
+    v.nobj = sc->object_count;
+    v.nruns = nruns;
+    v.fast_div = fast_div ? 1u : 0u;
+    v.neg_zero = make_float2(-0.0f, -0.0f);
+    v.width = cam.resolution_x;
+    v.height = cam.resolution_y;
+    for (int i = 0; i < 3; ++i) v.cam_pos[i] = cam.position[i];
+    for (int i = 0; i < 16; ++i) {
+        v.inv_view[i] = cam.inverse_view_matrix[i];
+        v.inv_proj[i] = cam.inverse_proj_matrix[i];
+    }
+    v.world_kind = sc->world.kind;
+    for (int i = 0; i < 3; ++i) {
+        v.top[i] = sc->world.top_color[i];
+        v.bottom[i] = sc->world.bottom_color[i];
+        v.solid[i] = sc->world.solid_color[i];
+    }
+}
+
+void free_batch(rdc_ctx* ctx);
+rdc_status capture_batch_graph(rdc_ctx* ctx);
 
 }  // namespace
 
@@ -149,6 +224,7 @@ void rdc_destroy(rdc_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_batch(ctx);
     cudaFree(ctx->d_rec);
     cudaFree(ctx->d_hit);
     cudaFree(ctx->d_mat);
@@ -183,27 +259,9 @@ rdc_status rdc_synchronize(rdc_ctx* ctx) {
 rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
     if (!sc) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: scene is NULL");
+    if (rdc_status st = check_scene(ctx, sc, "rdc_scene_upload")) return st;
     const rdc_camera& cam = sc->camera;
-    if (cam.resolution_x == 0 || cam.resolution_y == 0)
-        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: zero resolution");
-    if (cam.resolution_x > RDC_MAX_RESOLUTION || cam.resolution_y > RDC_MAX_RESOLUTION)
-        return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: resolution above RDC_MAX_RESOLUTION");
-    if (sc->object_count > RDC_MAX_OBJECTS)
-        return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: object_count " + std::to_string(sc->object_count) +
-                                            " above RDC_MAX_OBJECTS");
-    if (sc->object_count > 0 && !sc->objects)
-        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: objects is NULL");
-    if (sc->world.kind == RDC_WORLD_TRANSPARENT)
-        return fail(ctx, RDC_ERR_UNSUPPORTED,
-                    "rdc_scene_upload: World::Transparent is not supported (todo!() in the reference)");
-    if (sc->world.kind > RDC_WORLD_TRANSPARENT)
-        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_scene_upload: unknown world kind");
-
     const uint32_t n = sc->object_count;
-    for (uint32_t i = 0; i < n; ++i)
-        if (sc->objects[i].geometry != RDC_GEOMETRY_SPHERE && sc->objects[i].geometry != RDC_GEOMETRY_CUBE)
-            return fail(ctx, RDC_ERR_INVALID_ARGUMENT,
-                        "rdc_scene_upload: object " + std::to_string(i) + " has unknown geometry");
     const rdc::FlatCounts fc = rdc::flat_counts(sc);
     if (rdc::render_smem_bytes(fc.nrec, fc.nruns) > kMaxSceneSmem)
         return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: scene records exceed the shared-memory budget");
@@ -235,29 +293,7 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     // Host staging vectors die at return: wait for the copies.
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
-    rdc::SceneView& v = ctx->view;
-    v.rec = ctx->d_rec;
-    v.nrec = fc.nrec;
-    v.hit = ctx->d_hit;
-    v.mat = ctx->d_mat;
-    v.runs = ctx->d_runs;
-    v.nobj = n;
-    v.nruns = fc.nruns;
-    v.fast_div = fast_div ? 1u : 0u;
-    v.neg_zero = make_float2(-0.0f, -0.0f);
-    v.width = cam.resolution_x;
-    v.height = cam.resolution_y;
-    for (int i = 0; i < 3; ++i) v.cam_pos[i] = cam.position[i];
-    for (int i = 0; i < 16; ++i) {
-        v.inv_view[i] = cam.inverse_view_matrix[i];
-        v.inv_proj[i] = cam.inverse_proj_matrix[i];
-    }
-    v.world_kind = sc->world.kind;
-    for (int i = 0; i < 3; ++i) {
-        v.top[i] = sc->world.top_color[i];
-        v.bottom[i] = sc->world.bottom_color[i];
-        v.solid[i] = sc->world.solid_color[i];
-    }
+    fill_view(ctx->view, sc, ctx->d_rec, fc.nrec, ctx->d_hit, ctx->d_mat, ctx->d_runs, fc.nruns, fast_div);
 
     // Frame buffer follows the resolution (CpuRenderer::frame_buffer, cpu.rs:400-417).
     if (!ctx->d_accum || ctx->width != cam.resolution_x || ctx->height != cam.resolution_y) {
@@ -491,6 +527,259 @@ rdc_status rdc_scatter_fixed(rdc_ctx* ctx, const float* origins, const float* di
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     cudaFree(buf);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "rdc_scatter_fixed");
+    return RDC_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batch --
+namespace {
+
+void free_batch(rdc_ctx* ctx) {
+    auto& b = ctx->batch;
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    if (b.graph) cudaGraphDestroy(b.graph);
+    cudaFree(b.d_scenes);
+    cudaFree(b.d_rec);
+    cudaFree(b.d_hit);
+    cudaFree(b.d_mat);
+    cudaFree(b.d_runs);
+    cudaFree(b.d_accum);
+    cudaFree(b.d_pixel_counters);
+    b = rdc_ctx::Batch();
+}
+
+// Capture clear + persistent batch kernel into the batch graph.
+rdc_status capture_batch_graph(rdc_ctx* ctx) {
+    auto& b = ctx->batch;
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    if (b.graph) cudaGraphDestroy(b.graph);
+    b.exec = nullptr;
+    b.graph = nullptr;
+    int per_sm = 0;
+    RDC_CUDA(ctx, rdc::batch_occupancy((int)b.cfg.block_size, b.smem, &per_sm));
+    if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_batch: block size does not fit on an SM");
+    const int blocks = b.cfg.blocks_per_sm == 0 ? per_sm : std::min<int>(per_sm, (int)b.cfg.blocks_per_sm);
+    const int grid = ctx->num_sms * blocks;
+    rdc::BatchParams p;
+    p.scenes = b.d_scenes;
+    p.nscenes = b.n;
+    p.refill_min = b.cfg.refill_min_idle;
+    p.pixel_counters = b.d_pixel_counters;
+    p.segments = ctx->d_counters + 1;
+    RDC_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(b.d_accum, 0, b.accum_total * sizeof(float4), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.d_pixel_counters, 0, b.n * sizeof(uint32_t), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counters, 0, 2 * sizeof(unsigned long long), ctx->stream);
+    if (e == cudaSuccess) e = rdc::launch_batch(p, grid, (int)b.cfg.block_size, b.smem, ctx->stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(ctx, e, "rdc_batch: capture");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
+    b.graph = g;
+    RDC_CUDA(ctx, cudaGraphInstantiate(&b.exec, b.graph, 0));
+    return RDC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rdc_status rdc_batch_upload(rdc_ctx* ctx, const rdc_batch_item* items, uint32_t count) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!items || count == 0) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_upload: no items");
+    for (uint32_t i = 0; i < count; ++i) {
+        if (rdc_status st = check_scene(ctx, items[i].scene, "rdc_batch_upload: item " + std::to_string(i)))
+            return st;
+        if (items[i].max_bounces > RDC_MAX_BOUNCES)
+            return fail(ctx, RDC_ERR_LIMIT, "rdc_batch_upload: item " + std::to_string(i) + " max_bounces above limit");
+    }
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const rdc_launch_config cfg = ctx->batch.cfg;
+    free_batch(ctx);
+    auto& b = ctx->batch;
+    b.cfg = cfg;
+
+    // Sizes and offsets of every scene's arrays in the concatenated buffers.
+    std::vector<rdc::FlatCounts> fc(count);
+    std::vector<size_t> rec_off(count), obj_off(count), run_off(count);
+    size_t nrec = 0, nobj = 0, nruns = 0, accum = 0;
+    std::vector<double> work(count);
+    double total_work = 0.0;
+    b.accum_off.resize(count);
+    b.width.resize(count);
+    b.height.resize(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const rdc_scene_desc* sc = items[i].scene;
+        fc[i] = rdc::flat_counts(sc);
+        rec_off[i] = nrec;
+        obj_off[i] = nobj;
+        run_off[i] = nruns;
+        nrec += fc[i].nrec;
+        nobj += fc[i].nobj;
+        nruns += fc[i].nruns;
+        b.smem = std::max(b.smem, rdc::render_smem_bytes(fc[i].nrec, fc[i].nruns));
+        if (b.smem > kMaxSceneSmem) {
+            free_batch(ctx);
+            return fail(ctx, RDC_ERR_LIMIT,
+                        "rdc_batch_upload: item " + std::to_string(i) + " exceeds the shared-memory budget");
+        }
+        b.width[i] = sc->camera.resolution_x;
+        b.height[i] = sc->camera.resolution_y;
+        b.accum_off[i] = accum;
+        const size_t npix = (size_t)b.width[i] * b.height[i];
+        accum += npix;
+        b.paths += (uint64_t)npix * items[i].spp;
+        // estimated work: paths x (1 + a few segments) x objects tested
+        work[i] = (double)npix * items[i].spp * (1.0 + std::min<uint32_t>(items[i].max_bounces, 3u)) *
+                  (8.0 + sc->object_count);
+        total_work += work[i];
+    }
+    b.n = count;
+    b.accum_total = accum;
+
+    std::vector<float4> rec(std::max<size_t>(nrec, 1), make_float4(0, 0, 0, 0));
+    std::vector<float4> hit(std::max<size_t>(nobj, 1), make_float4(0, 0, 0, 0));
+    std::vector<MatDev> mat(std::max<size_t>(nobj, 1));
+    std::vector<int4> runs(std::max<size_t>(nruns, 1), make_int4(0, 0, 0, 0));
+    std::vector<char> fast(count);
+    for (uint32_t i = 0; i < count; ++i)
+        fast[i] = rdc::flatten(items[i].scene, rec.data() + rec_off[i], hit.data() + obj_off[i],
+                               mat.data() + obj_off[i], runs.data() + run_off[i]);
+
+    cudaError_t e = cudaMalloc((void**)&b.d_rec, rec.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_hit, hit.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_mat, mat.size() * sizeof(MatDev));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_runs, runs.size() * sizeof(int4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_accum, b.accum_total * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_pixel_counters, count * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_scenes, count * sizeof(rdc::BatchScene));
+    if (e != cudaSuccess) {
+        free_batch(ctx);
+        return cuda_fail(ctx, e, "rdc_batch_upload: cudaMalloc");
+    }
+    std::vector<rdc::BatchScene> scenes(count);
+    double acc_work = 0.0;
+    for (uint32_t i = 0; i < count; ++i) {
+        rdc::BatchScene& bs = scenes[i];
+        fill_view(bs.sc, items[i].scene, b.d_rec + rec_off[i], fc[i].nrec, b.d_hit + obj_off[i],
+                  b.d_mat + obj_off[i], b.d_runs + run_off[i], fc[i].nruns, fast[i] != 0);
+        bs.accum = b.d_accum + b.accum_off[i];
+        bs.npix = b.width[i] * b.height[i];
+        bs.spp = items[i].spp;
+        bs.max_bounces = items[i].max_bounces;
+        bs.key0 = (uint32_t)items[i].seed;
+        bs.key1 = (uint32_t)(items[i].seed >> 32);
+        bs.work_begin = (float)(acc_work / total_work);
+        acc_work += work[i];
+        if (bs.spp == 0) bs.npix = 0;  // nothing to render: the pool starts empty
+    }
+    e = cudaMemcpyAsync(b.d_rec, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_hit, hit.data(), hit.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_mat, mat.data(), mat.size() * sizeof(MatDev), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_runs, runs.data(), runs.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b.d_scenes, scenes.data(), count * sizeof(rdc::BatchScene), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        free_batch(ctx);
+        return cuda_fail(ctx, e, "rdc_batch_upload: copy");
+    }
+    ctx->h2d_bytes += rec.size() * sizeof(float4) + hit.size() * sizeof(float4) + mat.size() * sizeof(MatDev) +
+                      runs.size() * sizeof(int4) + count * sizeof(rdc::BatchScene);
+    if (rdc_status st = capture_batch_graph(ctx)) {
+        free_batch(ctx);
+        return st;
+    }
+    return RDC_OK;
+}
+
+rdc_status rdc_batch_render(rdc_ctx* ctx) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->batch.exec) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_batch_render: no batch uploaded");
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    RDC_CUDA(ctx, cudaGraphLaunch(ctx->batch.exec, ctx->stream));
+    RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->last_timed = true;
+    ctx->last_launches = 1;
+    ctx->last_paths = ctx->batch.paths;
+    return RDC_OK;
+}
+
+rdc_status rdc_batch_read_accum(rdc_ctx* ctx, uint32_t index, float* rgba_out, size_t count) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    auto& b = ctx->batch;
+    if (!b.exec) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_batch_read_accum: no batch uploaded");
+    if (index >= b.n) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_read_accum: index out of range");
+    const size_t need = (size_t)b.width[index] * b.height[index] * 4;
+    if (!rgba_out || count < need)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_read_accum: output smaller than width*height*4");
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaMemcpyAsync(rgba_out, b.d_accum + b.accum_off[index], need * sizeof(float),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->d2h_bytes += need * sizeof(float);
+    return RDC_OK;
+}
+
+rdc_status rdc_batch_set_config(rdc_ctx* ctx, const rdc_launch_config* config) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!config) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_set_config: NULL config");
+    if (config->block_size != 64 && config->block_size != 128 && config->block_size != 256)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_set_config: block_size must be 64, 128 or 256");
+    if (config->refill_min_idle < 1 || config->refill_min_idle > 32)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_set_config: refill_min_idle must be in 1..32");
+    if (rdc_status st = set_device(ctx)) return st;
+    ctx->batch.cfg = *config;
+    if (ctx->batch.n == 0) return RDC_OK;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return capture_batch_graph(ctx);
+}
+
+rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config) {
+    if (!ctx || !config) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_batch_get_config: NULL argument");
+    *config = ctx->batch.cfg;
+    return RDC_OK;
+}
+
+rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* best_ms_out) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->batch.exec) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_batch_autotune: no batch uploaded");
+    if (rdc_status st = set_device(ctx)) return st;
+    const uint32_t blocks[] = {128, 256};
+    const uint32_t refills[] = {1, 4, 16};
+    rdc_launch_config best = ctx->batch.cfg;
+    float best_ms = 0.0f;
+    bool have = false;
+    for (uint32_t bsz : blocks) {
+        int per_sm = 0;
+        RDC_CUDA(ctx, rdc::batch_occupancy((int)bsz, ctx->batch.smem, &per_sm));
+        for (int bps = std::max(1, per_sm - 1); bps <= per_sm; ++bps) {
+            for (uint32_t rf : refills) {
+                const rdc_launch_config c{bsz, (uint32_t)bps, rf};
+                if (rdc_status st = rdc_batch_set_config(ctx, &c)) return st;
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2; ++rep) {  // first run warms up
+                    if (rdc_status st = rdc_batch_render(ctx)) return st;
+                    RDC_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+                    RDC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+                }
+                if (!have || ms < best_ms) {
+                    best = c;
+                    best_ms = ms;
+                    have = true;
+                }
+            }
+        }
+    }
+    if (rdc_status st = rdc_batch_set_config(ctx, &best)) return st;
+    if (best_out) *best_out = best;
+    if (best_ms_out) *best_ms_out = best_ms;
     return RDC_OK;
 }
 

@@ -468,4 +468,57 @@ __device__ __forceinline__ void primary_ray(const SceneView& sc, uint32_t x, uin
     d = vneg(vnormalize(mk(wd[0], wd[1], wd[2])));
 }
 
+// --------------------------------------------------------------- a path ---
+struct PathState {
+    V3 o, d, atten, light;
+    uint32_t bounce;
+};
+
+__device__ __forceinline__ void path_start(const SceneView& sc, uint32_t pix, PathState& s) {
+    primary_ray(sc, pix % sc.width, pix / sc.width, s.o, s.d);
+    s.atten = mk(1.f, 1.f, 1.f);
+    s.light = mk(0.f, 0.f, 0.f);
+    s.bounce = 0;
+}
+
+// One segment of a path (src/renderer/cpu.rs:256-338): trace_ray, then the
+// scatter of a hit or the world sample of a miss.  `rec`/`runs` are the
+// scene's intersection records (shared or global memory).  Returns true when
+// the path has ended (a miss, or max_bounces segments traced).
+__device__ __forceinline__ bool path_segment(const SceneView& sc, const float4* __restrict__ rec,
+                                             const int4* __restrict__ runs, PathState& s, uint32_t pix,
+                                             uint32_t sample, uint32_t max_bounces, uint32_t stream_id,
+                                             uint32_t k0, uint32_t k1, uint32_t& segs) {
+    if (s.bounce >= max_bounces) return true;  // max_bounces == 0: the path adds (0, 0, 0, 1)
+    ++segs;
+    const RayPre r = ray_pre(s.o, s.d, sc.neg_zero);
+    float t;
+    int idx;
+    intersect_all(rec, runs, (int)sc.nruns, sc.fast_div != 0u, r, t, idx);
+    if (idx < 0) {
+        const V3 sky = world_sample(sc, s.d);
+        s.light = vadd(s.light, mk(sky.x * s.atten.x, sky.y * s.atten.y, sky.z * s.atten.z));
+        return true;
+    }
+    const float4 hi = __ldg(&sc.hit[idx]);
+    const MatDev m = sc.mat[idx];
+    const HitRec h = closest_hit(s.o, s.d, t, hi, __float_as_int(m.d.y));
+    uint32_t w[12];
+    const uint32_t c2 = s.bounce * 4u;
+    const U4 w0 = philox(pix, sample, c2, stream_id, k0, k1);
+    const U4 w1 = philox(pix, sample, c2 + 1u, stream_id, k0, k1);
+    const U4 w2 = philox(pix, sample, c2 + 2u, stream_id, k0, k1);
+    w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
+    w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
+    w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
+    V3 no, nd;
+    scatter(s.d, h, m, w, no, nd);
+    s.o = no;
+    s.d = nd;
+    s.atten = mk(s.atten.x * m.a.x, s.atten.y * m.a.y, s.atten.z * m.a.z);
+    s.light = vadd(s.light, mk(m.b.x, m.b.y, m.b.z));
+    ++s.bounce;
+    return s.bounce >= max_bounces;
+}
+
 }  // namespace rdc

@@ -65,10 +65,33 @@ struct RenderParams {
     unsigned long long* segments;
 };
 
+// One scene of a batch (rdc_batch_upload): its view, accumulator, sample
+// count, bounce limit, RNG key and share of the batch's estimated work.
+struct BatchScene {
+    SceneView sc;
+    float4* accum;
+    uint32_t npix;
+    uint32_t spp;
+    uint32_t max_bounces;
+    uint32_t key0;
+    uint32_t key1;
+    float work_begin;  // cumulative estimated work before this scene, in [0, 1)
+};
+
+struct BatchParams {
+    const BatchScene* scenes;
+    uint32_t nscenes;
+    uint32_t refill_min;      // idle lanes of a warp that trigger a refill (regroup period)
+    uint32_t* pixel_counters; // per scene: next pixel to hand out
+    unsigned long long* segments;
+};
+
 // Kernel launchers (rdc_kernels.cu).  Each returns the cudaError_t of its
 // launch.
 cudaError_t launch_render(const RenderParams& p, int grid, int block, size_t smem, cudaStream_t s);
 cudaError_t render_occupancy(int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_batch(const BatchParams& p, int grid, int block, size_t smem, cudaStream_t s);
+cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_tonemap(const float4* accum, uint32_t npix, uint32_t sample_count, uchar4* out,
                            cudaStream_t s);
 cudaError_t launch_intersect_rays(const SceneView& sc, const float* o, const float* d, uint32_t n,

@@ -28,11 +28,12 @@ __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderPar
 
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int nruns = (int)P.sc.nruns;
 
     int pix = -1;
-    uint32_t sample = 0, send = 0, bounce = 0;
-    V3 o = mk(0.f, 0.f, 0.f), d = o, atten = o, light = o;
+    uint32_t sample = 0, send = 0;
+    PathState st;
+    st.o = st.d = st.atten = st.light = mk(0.f, 0.f, 0.f);
+    st.bounce = 0;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t segs = 0;
     bool pool_open = true;
@@ -52,57 +53,20 @@ __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderPar
                 if (mine < P.npix) {
                     pix = (int)mine;
                     acc = P.accum[pix];
-                    primary_ray(P.sc, mine % P.sc.width, mine / P.sc.width, o, d);
+                    path_start(P.sc, mine, st);
                     sample = P.s0;
                     send = P.s0 + P.nspp;
-                    bounce = 0;
-                    atten = mk(1.f, 1.f, 1.f);
-                    light = mk(0.f, 0.f, 0.f);
                 }
             }
         }
         if (__ballot_sync(FULL, pix >= 0) == 0u) break;
         if (pix < 0) continue;  // idle lane: rejoins the warp at the refill ballot
 
-        bool done;
-        if (bounce < P.max_bounces) {
-            ++segs;
-            const RayPre r = ray_pre(o, d, P.sc.neg_zero);
-            float t;
-            int idx;
-            intersect_all(s_rec, s_runs, nruns, P.sc.fast_div != 0u, r, t, idx);
-            if (idx >= 0) {
-                const float4 hi = __ldg(&P.sc.hit[idx]);
-                const MatDev m = P.sc.mat[idx];
-                const HitRec h = closest_hit(o, d, t, hi, __float_as_int(m.d.y));
-                uint32_t w[12];
-                const uint32_t c2 = bounce * 4u;
-                const U4 w0 = philox(pix, sample, c2, P.stream_id, P.key0, P.key1);
-                const U4 w1 = philox(pix, sample, c2 + 1u, P.stream_id, P.key0, P.key1);
-                w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
-                w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
-                const U4 w2 = philox(pix, sample, c2 + 2u, P.stream_id, P.key0, P.key1);
-                w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
-                V3 no, nd;
-                scatter(d, h, m, w, no, nd);
-                o = no;
-                d = nd;
-                atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
-                light = vadd(light, mk(m.b.x, m.b.y, m.b.z));
-                ++bounce;
-                done = bounce >= P.max_bounces;
-            } else {
-                const V3 sky = world_sample(P.sc, d);
-                light = vadd(light, mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z));
-                done = true;
-            }
-        } else {
-            done = true;  // max_bounces == 0: the path adds (0, 0, 0, 1)
-        }
-        if (done) {
-            acc.x = acc.x + light.x;
-            acc.y = acc.y + light.y;
-            acc.z = acc.z + light.z;
+        if (path_segment(P.sc, s_rec, s_runs, st, (uint32_t)pix, sample, P.max_bounces, P.stream_id, P.key0,
+                         P.key1, segs)) {
+            acc.x = acc.x + st.light.x;
+            acc.y = acc.y + st.light.y;
+            acc.z = acc.z + st.light.z;
             acc.w = acc.w + 1.0f;
             ++sample;
             if (sample == send) {
@@ -111,15 +75,143 @@ __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderPar
             } else {
                 // Next sample of the same pixel: the primary ray is recomputed
                 // (identical every sample) rather than kept in registers.
-                primary_ray(P.sc, (uint32_t)pix % P.sc.width, (uint32_t)pix / P.sc.width, o, d);
-                atten = mk(1.f, 1.f, 1.f);
-                light = mk(0.f, 0.f, 0.f);
-                bounce = 0;
+                path_start(P.sc, (uint32_t)pix, st);
             }
         }
     }
 
     // Segment counter: warp sum, one 64-bit atomic per warp.
+    unsigned long long s = segs;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
+    if (lane == 0 && s != 0ull) atomicAdd(P.segments, s);
+}
+
+// Many scenes in one persistent launch.  A block works on one scene at a
+// time: it stages that scene's records and view in shared memory, and its
+// warps run render_kernel's loop over the scene's pixel pool (one lane per
+// pixel for all of the scene's samples).  Blocks start on scenes in
+// proportion to each scene's estimated work; a block whose scene pool is
+// empty waits for its warps to finish their pixels, then moves to the scene
+// with the most pixels left.  RNG stream = batch index.
+__device__ __forceinline__ int batch_initial_scene(const BatchParams& P, float pos, int lane) {
+    int count = 0;  // scenes whose work starts at or before pos
+    for (uint32_t base = 0; base < P.nscenes; base += 32) {
+        const uint32_t s = base + lane;
+        const bool le = s < P.nscenes && P.scenes[s].work_begin <= pos;
+        count += __popc(__ballot_sync(0xffffffffu, le));
+    }
+    return count > 0 ? count - 1 : 0;
+}
+
+// The scene with the most pixels not yet handed out (lowest index on ties),
+// or -1 when every pool is empty.  Called by one full warp.
+__device__ __forceinline__ int batch_busiest_scene(const BatchParams& P, int lane) {
+    uint32_t best = 0;
+    int best_s = -1;
+    for (uint32_t s = lane; s < P.nscenes; s += 32) {
+        const uint32_t taken = *reinterpret_cast<volatile const uint32_t*>(&P.pixel_counters[s]);
+        const uint32_t npix = P.scenes[s].npix;
+        const uint32_t left = taken < npix ? npix - taken : 0u;
+        if (left > best) {
+            best = left;
+            best_s = (int)s;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const uint32_t ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int os = __shfl_xor_sync(0xffffffffu, best_s, off);
+        if (ob > best || (ob == best && ob != 0u && (unsigned)os < (unsigned)best_s)) {
+            best = ob;
+            best_s = os;
+        }
+    }
+    return best > 0u ? best_s : -1;
+}
+
+__global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParams P) {
+    extern __shared__ float4 smem[];
+    __shared__ BatchScene s_bs;
+    __shared__ int s_scene;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        const int sc0 = batch_initial_scene(P, ((float)blockIdx.x + 0.5f) / (float)gridDim.x, lane);
+        if (lane == 0) s_scene = sc0;
+    }
+    __syncthreads();
+    uint32_t segs = 0;
+
+    for (;;) {
+        const int scene = s_scene;
+        if (scene < 0) break;
+        // Stage the scene: view, then records and runs.
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(P.scenes + scene);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&s_bs);
+            for (uint32_t i = threadIdx.x; i < sizeof(BatchScene) / 4; i += blockDim.x) dst[i] = src[i];
+        }
+        __syncthreads();
+        float4* s_rec = smem;
+        int4* s_runs = reinterpret_cast<int4*>(smem + s_bs.sc.nrec);
+        for (uint32_t i = threadIdx.x; i < s_bs.sc.nrec; i += blockDim.x) s_rec[i] = s_bs.sc.rec[i];
+        for (uint32_t i = threadIdx.x; i < s_bs.sc.nruns; i += blockDim.x) s_runs[i] = s_bs.sc.runs[i];
+        __syncthreads();
+
+        const uint32_t npix = s_bs.npix;
+        uint32_t* counter = P.pixel_counters + scene;
+        int pix = -1;
+        uint32_t sample = 0;
+        PathState st;
+        st.o = st.d = st.atten = st.light = mk(0.f, 0.f, 0.f);
+        st.bounce = 0;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool pool_open = true;
+        for (;;) {
+            const unsigned need = __ballot_sync(FULL, pix < 0);
+            if (need != 0u && pool_open && (__popc(need) >= P.refill_min || need == FULL)) {
+                const unsigned cnt = __popc(need);
+                const int leader = __ffs(need) - 1;
+                unsigned base = 0;
+                if (lane == leader) base = atomicAdd(counter, cnt);
+                base = __shfl_sync(FULL, base, leader);
+                if (base + cnt >= npix) pool_open = false;
+                if (pix < 0) {
+                    const unsigned mine = base + __popc(need & ((1u << lane) - 1u));
+                    if (mine < npix) {
+                        pix = (int)mine;
+                        acc = s_bs.accum[pix];
+                        path_start(s_bs.sc, mine, st);
+                        sample = 0;
+                    }
+                }
+            }
+            if (__ballot_sync(FULL, pix >= 0) == 0u && !pool_open) break;
+            if (pix < 0) continue;
+            if (path_segment(s_bs.sc, s_rec, s_runs, st, (uint32_t)pix, sample, s_bs.max_bounces,
+                             (uint32_t)scene, s_bs.key0, s_bs.key1, segs)) {
+                acc.x = acc.x + st.light.x;
+                acc.y = acc.y + st.light.y;
+                acc.z = acc.z + st.light.z;
+                acc.w = acc.w + 1.0f;
+                ++sample;
+                if (sample == s_bs.spp) {
+                    s_bs.accum[pix] = acc;
+                    pix = -1;
+                } else {
+                    path_start(s_bs.sc, (uint32_t)pix, st);
+                }
+            }
+        }
+        __syncthreads();  // every warp is done with this scene
+        if (threadIdx.x < 32) {
+            const int nxt = batch_busiest_scene(P, lane);
+            if (lane == 0) s_scene = nxt;
+        }
+        __syncthreads();
+    }
+
     unsigned long long s = segs;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
@@ -230,6 +322,18 @@ cudaError_t render_occupancy(int block, size_t smem, int* blocks_per_sm) {
                                          (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, render_kernel, block, smem);
+}
+
+cudaError_t launch_batch(const BatchParams& p, int grid, int block, size_t smem, cudaStream_t s) {
+    batch_kernel<<<grid, block, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_kernel, block, smem);
 }
 
 cudaError_t launch_tonemap(const float4* accum, uint32_t npix, uint32_t sample_count, uchar4* out,

@@ -79,6 +79,15 @@ class RdcStats(C.Structure):
     ]
 
 
+class RdcBatchItem(C.Structure):
+    _fields_ = [("scene", C.POINTER(RdcSceneDesc)), ("spp", C.c_uint32), ("max_bounces", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+class RdcLaunchConfig(C.Structure):
+    _fields_ = [("block_size", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("refill_min_idle", C.c_uint32)]
+
+
 # name -> (restype, argtypes).  Every exported symbol of include/raydar_cuda.h.
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
@@ -95,6 +104,12 @@ SIGNATURES = {
     "rdc_render_static": (C.c_int, [C.POINTER(RdcSceneDesc), C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                     C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64), C.c_char_p, C.c_size_t]),
     "rdc_read_accum": (C.c_int, [_P, _FP, C.c_size_t]),
+    "rdc_batch_upload": (C.c_int, [_P, C.POINTER(RdcBatchItem), C.c_uint32]),
+    "rdc_batch_render": (C.c_int, [_P]),
+    "rdc_batch_read_accum": (C.c_int, [_P, C.c_uint32, _FP, C.c_size_t]),
+    "rdc_batch_set_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
+    "rdc_batch_get_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
+    "rdc_batch_autotune": (C.c_int, [_P, C.POINTER(RdcLaunchConfig), C.POINTER(C.c_float)]),
     "rdc_write_accum": (C.c_int, [_P, _FP, C.c_size_t, C.c_uint32]),
     "rdc_read_rgba8": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint8), C.c_size_t]),
     "rdc_stats_get": (C.c_int, [_P, C.POINTER(RdcStats)]),

@@ -60,20 +60,23 @@ def _ground(half_extent: float = 10.0) -> Object:
                   Material(albedo=np.array([0.5, 0.5, 0.5], np.float32), roughness=1.0))
 
 
-def _place(rng, radii, extent, placed, inset=True, max_tries=2000):
+def _place(rng, radii, extent, placed, inset=True, strict=True, max_tries=2000):
     """Rejection-sample non-overlapping footprints (x, z): centres in
-    [-extent + r, extent - r] (inset) or [-extent, extent]."""
+    [-extent + r, extent - r] (inset) or [-extent, extent].  With strict=False
+    an object that finds no free spot in max_tries keeps its last draw (dense
+    batch scenes cannot all fit on the ground without touching)."""
     out = []
     for r in radii:
         lo, hi = (-extent + r, extent - r) if inset else (-extent, extent)
         for _ in range(max_tries):
             x, z = rng.uniform(lo, hi, 2)
             if all((x - px) ** 2 + (z - pz) ** 2 >= (r + pr) ** 2 for px, pz, pr in placed):
-                placed.append((x, z, r))
-                out.append((x, z))
                 break
         else:
-            raise RuntimeError("could not place object without overlap")
+            if strict:
+                raise RuntimeError("could not place object without overlap")
+        placed.append((x, z, r))
+        out.append((x, z))
     return out
 
 
@@ -102,14 +105,14 @@ def _mix_kinds(rng, n, mix=(("D", 0.40), ("M", 0.25), ("G", 0.20), ("S", 0.15)))
 
 
 def c2_default(seed: int = 2, width: int = 1920, height: int = 1080, n_spheres: int = 64,
-               n_cubes: int = 16) -> Workload:
+               n_cubes: int = 16, max_tries: int = 2000) -> Workload:
     rng = np.random.default_rng(seed)
     radii = np.exp(rng.uniform(np.log(0.1), np.log(1.5), n_spheres))
     edges = rng.uniform(0.3, 2.0, n_cubes)
     placed: list = []
     # footprints: spheres by radius, cubes by their half diagonal
-    xz_s = _place(rng, radii, 10.0, placed)
-    xz_c = _place(rng, edges * np.sqrt(0.5), 10.0, placed)
+    xz_s = _place(rng, radii, 10.0, placed, strict=False, max_tries=max_tries)
+    xz_c = _place(rng, edges * np.sqrt(0.5), 10.0, placed, strict=False, max_tries=max_tries)
     kinds = _mix_kinds(rng, n_spheres + n_cubes)
     objs = [_ground()]
     for i, (r, (x, z)) in enumerate(zip(radii, xz_s)):
@@ -133,7 +136,8 @@ def c3_batch(seed: int = 3, count: int = 64) -> list[Workload]:
         bounces = int(rng.integers(4, 13))
         ns = int(rng.integers(4, 201))
         nc = int(rng.integers(0, 21))
-        sub = c2_default(seed=int(rng.integers(1 << 30)), width=w, height=h, n_spheres=ns, n_cubes=nc)
+        sub = c2_default(seed=int(rng.integers(1 << 30)), width=w, height=h, n_spheres=ns, n_cubes=nc,
+                         max_tries=200)
         out.append(Workload(f"c3_scene{k:02d}", sub.scene, spp, bounces))
     return out
 
