@@ -57,6 +57,7 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batch", action="store_true", help="skip the batched (config 3) measurement")
     p.add_argument("--batch-only", action="store_true", help="only the batched (config 3) measurement")
+    p.add_argument("--no-large", action="store_true", help="skip the LBVH (config 5) measurement")
     p.add_argument("--batch-spp-div", type=int, default=1, help="divide every batch item's spp (small profiling case)")
     return p.parse_args()
 
@@ -280,6 +281,57 @@ def batch_bench(local: int, steps: int, spp_div: int = 1):
     }
 
 
+def lbvh_bench(local: int, steps: int, peak_tflops: float):
+    """Config 5 forward: 100k spheres + 10k cubes, device-built LBVH, one
+    1920x1080 frame of 256 spp / 12 bounces per step.  Ops/segment follow the
+    LBVH model 30 * node visits + 24 * object tests + 100, with the visit and
+    test counts measured by the kernel in the same launches."""
+    from raydar_gb300 import CudaRenderer, RendererConfig, native, scenegen
+
+    w = scenegen.c5_large()
+    r = CudaRenderer(RendererConfig(max_sample_count=w.spp, max_bounces=w.max_bounces), device=local, seed=0)
+    t0 = time.perf_counter()
+    r.upload(w.scene)
+    build_s = time.perf_counter() - t0
+    st = r.stats()
+    depth = st.bvh_depth
+    r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+    r.render_range(0, w.spp)  # warm-up frame
+    r.stats()
+    segs = visits = tests = 0
+    dev_ms = 0.0
+    t0 = time.perf_counter()
+    for k in range(steps):
+        r.seed = 7000 + k
+        r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+        r.render_range(0, w.spp)
+        st = r.stats()
+        segs += st.segments
+        visits += st.node_visits
+        tests += st.prim_tests
+        dev_ms += st.device_ms
+    wall = time.perf_counter() - t0
+    r.close()
+    v_per = visits / segs
+    t_per = tests / segs
+    ops = 30 * v_per + 24 * t_per + 100
+    achieved = ops * segs / (dev_ms / 1e3) / 1e12
+    return {
+        "workload": "c5_large: 100k spheres r in [0.01,0.2] + 10k cubes edge in [0.02,0.3] in a 40x10x40 box, "
+                    "1920x1080, 256 spp, 12 bounces, device-built LBVH",
+        "segments_per_s": segs / wall,
+        "kernel_ms_per_frame": dev_ms / steps,
+        "node_visits_per_segment": v_per,
+        "object_tests_per_segment": t_per,
+        "ops_per_segment": ops,
+        "achieved_tflops": achieved,
+        "frac_of_peak": achieved / peak_tflops if peak_tflops else None,
+        "bvh_build_s": build_s,
+        "bvh_depth": depth,
+        "steps": steps,
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -398,6 +450,11 @@ def run_ours(args):
     if rank == 0 and not args.no_batch:
         batched = batch_bench(local, max(1, min(args.steps, 3)), args.batch_spp_div)
 
+    large = None
+    if rank == 0 and not args.no_large:
+        pk = max(ops_s.value / 1e12, n_sms * 128 * (clk.get("sm_mhz") or 0.0) * 1e6 / 1e12)
+        large = lbvh_bench(local, max(1, min(args.steps, 2)), pk)
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -444,6 +501,7 @@ def run_ours(args):
         "clocks": clk,
         "cpu_baseline": base,
         "batched": batched,
+        "large_scene": large,
     }
     print(json.dumps(line), flush=True)
 

@@ -56,8 +56,14 @@ enum { RDC_PROJECTION_PERSPECTIVE = 0, RDC_PROJECTION_ORTHOGRAPHIC = 1 };
 
 /* Documented maxima (checked on upload; RDC_ERR_LIMIT above them). */
 #define RDC_MAX_RESOLUTION 16384u     /* per axis */
-#define RDC_MAX_OBJECTS 4096u         /* brute-force path: geometry staged in shared memory */
+#define RDC_MAX_OBJECTS (1u << 24)    /* objects per scene */
+#define RDC_MAX_BRUTE_OBJECTS 4096u   /* brute-force render: records staged in shared memory */
 #define RDC_MAX_BOUNCES 1024u
+
+/* Closest-hit acceleration (rdc_set_accel).  Both give the reference's
+ * result bit for bit; the LBVH is built on the device on upload. */
+enum { RDC_ACCEL_AUTO = 0, RDC_ACCEL_BRUTE_FORCE = 1, RDC_ACCEL_LBVH = 2 };
+#define RDC_ACCEL_AUTO_LBVH_ABOVE 512u /* AUTO uses the LBVH above this many objects */
 
 /* Camera, field for field as src/scene/camera.rs:13-30.  The renderer uses
  * `position`, the resolution and the two inverse matrices as stored; the
@@ -126,6 +132,10 @@ typedef struct rdc_stats {
     uint32_t kernel_launches; /* kernels launched by the last render */
     uint64_t h2d_bytes;       /* host->device bytes the context has copied since creation */
     uint64_t d2h_bytes;       /* device->host bytes the context has copied since creation */
+    uint64_t node_visits;     /* LBVH interior nodes visited by the last render (0 for brute force) */
+    uint64_t prim_tests;      /* LBVH object tests of the last render (0 for brute force) */
+    uint32_t accel;           /* RDC_ACCEL_BRUTE_FORCE or RDC_ACCEL_LBVH: what the current scene uses */
+    uint32_t bvh_depth;       /* deepest LBVH leaf of the current scene (0 without an LBVH) */
 } rdc_stats;
 
 typedef struct rdc_ctx rdc_ctx;
@@ -160,6 +170,11 @@ rdc_status rdc_synchronize(rdc_ctx* ctx);
  * If the resolution changed, the accumulator is reallocated and zeroed, as
  * CpuRenderer::frame_buffer does (src/renderer/cpu.rs:400-417). */
 rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* scene);
+
+/* Choose the closest-hit acceleration (RDC_ACCEL_*) for this and later
+ * uploads; with a scene already uploaded, builds or drops its LBVH now.  The
+ * reference always tests every object (src/renderer/cpu.rs:344-352). */
+rdc_status rdc_set_accel(rdc_ctx* ctx, uint32_t mode);
 
 /* ---- rendering -------------------------------------------------------- */
 

@@ -54,6 +54,15 @@ struct rdc_ctx {
     int render_block = rdc::kRenderBlock;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
+    // closest-hit acceleration
+    uint32_t accel_mode = RDC_ACCEL_AUTO;
+    bool bvh_active = false;
+    uint32_t bvh_depth = 0;
+    rdc::BvhDevice bvh;
+    bool brute_fits = false;  // records + runs fit the shared-memory budget
+    std::vector<rdc_object> host_objects;  // copy of the uploaded scene (LBVH rebuilds)
+    rdc_scene_desc host_desc{};
+
     // batch (rdc_batch_upload)
     struct Batch {
         uint32_t n = 0;
@@ -168,6 +177,42 @@ void fill_view(rdc::SceneView& v, const rdc_scene_desc* sc, const float4* rec, u
 void free_batch(rdc_ctx* ctx);
 rdc_status capture_batch_graph(rdc_ctx* ctx);
 
+// Pick brute force or the LBVH for the stored scene and build / drop the LBVH.
+rdc_status apply_accel(rdc_ctx* ctx, bool scene_changed) {
+    const uint32_t n = ctx->host_desc.object_count;
+    bool want_bvh;
+    if (ctx->accel_mode == RDC_ACCEL_BRUTE_FORCE) {
+        want_bvh = false;  // rdc_render refuses it if the records do not fit shared memory
+    } else if (ctx->accel_mode == RDC_ACCEL_LBVH) {
+        want_bvh = true;
+    } else {
+        want_bvh = n > RDC_ACCEL_AUTO_LBVH_ABOVE || !ctx->brute_fits;
+    }
+    if (!want_bvh) {
+        ctx->bvh.release();
+        ctx->bvh_active = false;
+        ctx->bvh_depth = 0;
+        return RDC_OK;
+    }
+    if (ctx->bvh_active && !scene_changed) return RDC_OK;  // already built for this scene
+    uint32_t depth = 0;
+    const cudaError_t e = rdc::build_lbvh(&ctx->host_desc, ctx->bvh, ctx->stream, &depth);
+    if (e != cudaSuccess) {
+        ctx->bvh.release();
+        ctx->bvh_active = false;
+        return cuda_fail(ctx, e, "LBVH build");
+    }
+    if (depth > 64) {
+        ctx->bvh.release();
+        ctx->bvh_active = false;
+        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the 64-entry traversal stack");
+    }
+    ctx->bvh_active = n > 0;
+    ctx->bvh_depth = depth;
+    ctx->h2d_bytes += (uint64_t)n * 64;
+    return RDC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -225,6 +270,7 @@ void rdc_destroy(rdc_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_batch(ctx);
+    ctx->bvh.release();
     cudaFree(ctx->d_rec);
     cudaFree(ctx->d_hit);
     cudaFree(ctx->d_mat);
@@ -263,8 +309,7 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     const rdc_camera& cam = sc->camera;
     const uint32_t n = sc->object_count;
     const rdc::FlatCounts fc = rdc::flat_counts(sc);
-    if (rdc::render_smem_bytes(fc.nrec, fc.nruns) > kMaxSceneSmem)
-        return fail(ctx, RDC_ERR_LIMIT, "rdc_scene_upload: scene records exceed the shared-memory budget");
+    const bool brute_fits = n <= RDC_MAX_BRUTE_OBJECTS && rdc::render_smem_bytes(fc.nrec, fc.nruns) <= kMaxSceneSmem;
     std::vector<float4> rec(fc.nrec ? fc.nrec : 1, make_float4(0, 0, 0, 0));
     std::vector<float4> hit(n ? n : 1, make_float4(0, 0, 0, 0));
     std::vector<MatDev> mat(n ? n : 1);
@@ -294,6 +339,12 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
     fill_view(ctx->view, sc, ctx->d_rec, fc.nrec, ctx->d_hit, ctx->d_mat, ctx->d_runs, fc.nruns, fast_div);
+    ctx->brute_fits = brute_fits;
+    ctx->has_scene = false;
+    ctx->host_objects.assign(sc->objects, sc->objects + n);
+    ctx->host_desc = *sc;
+    ctx->host_desc.objects = ctx->host_objects.data();
+    if (rdc_status bst = apply_accel(ctx, true)) return bst;
 
     // Frame buffer follows the resolution (CpuRenderer::frame_buffer, cpu.rs:400-417).
     if (!ctx->d_accum || ctx->width != cam.resolution_x || ctx->height != cam.resolution_y) {
@@ -311,6 +362,21 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
         ctx->sample_count = 0;
     }
     ctx->has_scene = true;
+    return RDC_OK;
+}
+
+rdc_status rdc_set_accel(rdc_ctx* ctx, uint32_t mode) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (mode > RDC_ACCEL_LBVH) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_set_accel: unknown mode");
+    const uint32_t old_mode = ctx->accel_mode;
+    ctx->accel_mode = mode;
+    if (!ctx->has_scene) return RDC_OK;
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (rdc_status st = apply_accel(ctx, false)) {
+        ctx->accel_mode = old_mode;
+        return st;
+    }
     return RDC_OK;
 }
 
@@ -335,7 +401,7 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
     ctx->last_paths = (uint64_t)ctx->width * ctx->height * spp_count;
     ctx->last_launches = 0;
     ctx->last_timed = false;
-    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     if (spp_count == 0) return RDC_OK;
 
     rdc::RenderParams p;
@@ -351,9 +417,18 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
     p.work_counter = reinterpret_cast<uint32_t*>(ctx->d_counters);
     p.segments = ctx->d_counters + 1;
 
-    const size_t smem = rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
+    if (!ctx->bvh_active && !ctx->brute_fits)
+        return fail(ctx, RDC_ERR_LIMIT,
+                    "rdc_render: brute force needs the scene's records in shared memory (at most "
+                    "RDC_MAX_BRUTE_OBJECTS objects); use RDC_ACCEL_LBVH or RDC_ACCEL_AUTO");
+    p.bvh = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
+    p.bvh_counters = ctx->d_counters + 2;
+    const size_t smem = ctx->bvh_active ? 0 : rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
     int per_sm = 0;
-    RDC_CUDA(ctx, rdc::render_occupancy(ctx->render_block, smem, &per_sm));
+    if (ctx->bvh_active)
+        RDC_CUDA(ctx, rdc::render_bvh_occupancy(ctx->render_block, &per_sm));
+    else
+        RDC_CUDA(ctx, rdc::render_occupancy(ctx->render_block, smem, &per_sm));
     if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: scene does not fit in shared memory");
     const uint64_t warps_needed = ((uint64_t)p.npix + 31) / 32;
     uint64_t grid = (uint64_t)ctx->num_sms * per_sm;
@@ -361,7 +436,10 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
     if (grid > grid_needed) grid = grid_needed;
 
     RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-    RDC_CUDA(ctx, rdc::launch_render(p, (int)grid, ctx->render_block, smem, ctx->stream));
+    if (ctx->bvh_active)
+        RDC_CUDA(ctx, rdc::launch_render_bvh(p, (int)grid, ctx->render_block, ctx->stream));
+    else
+        RDC_CUDA(ctx, rdc::launch_render(p, (int)grid, ctx->render_block, smem, ctx->stream));
     RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->last_timed = true;
     ctx->last_launches = 1;
@@ -417,9 +495,13 @@ rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out) {
     if (!ctx || !out) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_stats_get: NULL argument");
     if (rdc_status st = set_device(ctx)) return st;
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    unsigned long long c[2] = {0, 0};
+    unsigned long long c[4] = {0, 0, 0, 0};
     RDC_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
     out->segments = c[1];
+    out->node_visits = c[2];
+    out->prim_tests = c[3];
+    out->accel = ctx->bvh_active ? RDC_ACCEL_LBVH : RDC_ACCEL_BRUTE_FORCE;
+    out->bvh_depth = ctx->bvh_depth;
     out->paths = ctx->last_paths;
     out->device_ms = 0.0f;
     if (ctx->last_timed) RDC_CUDA(ctx, cudaEventElapsedTime(&out->device_ms, ctx->ev0, ctx->ev1));
@@ -480,7 +562,9 @@ rdc_status rdc_intersect_rays(rdc_ctx* ctx, const float* origins, const float* d
     uint8_t* d_f = (uint8_t*)(buf + 3 * f3 + n * sizeof(float) + n * sizeof(int32_t));
     cudaError_t e = cudaMemcpyAsync(d_o, origins, f3, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, directions, f3, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = rdc::launch_intersect_rays(ctx->view, d_o, d_d, n, d_t, d_i, d_n, d_f, ctx->stream);
+    const rdc::BvhView bv = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
+    if (e == cudaSuccess)
+        e = rdc::launch_intersect_rays(ctx->view, bv, d_o, d_d, n, d_t, d_i, d_n, d_f, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, d_t, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(index_out, d_i, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(normal_out, d_n, f3, cudaMemcpyDeviceToHost, ctx->stream);

@@ -1,0 +1,276 @@
+// rdc_bvh.cu -- device build of the linear BVH used for large scenes.
+//
+//   1. object boxes and primitive records (host, exact reference constants)
+//   2. 30-bit Morton code of each box centre in the scene's centre bounds
+//   3. radix sort of (code, object) pairs (CUB)
+//   4. Karras, "Maximizing parallelism in the construction of BVHs, octrees
+//      and k-d trees" (HPG 2012): internal node i of N-1 finds its key range
+//      and split from the longest common prefixes of (code, position) keys
+//   5. bottom-up refit: each leaf walks towards the root; at every node the
+//      first arriving child records its box and stops (one atomic per node),
+//      the second computes the union and continues.  No thread ever waits.
+//   6. tree depth (must stay <= 64 for the traversal stack; Karras trees over
+//      30-bit codes with position tie-breaks are at most 62 deep).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "raydar_cuda.h"
+#include "rdc_bvh.cuh"
+#include "rdc_internal.hpp"
+
+namespace rdc {
+
+namespace {
+
+// Spread the low 10 bits of v so there are two zero bits between each.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void morton_kernel(const float4* __restrict__ box, uint32_t n, float3 lo, float3 inv_ext,
+                              uint32_t* keys, uint32_t* vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = box[2 * i], b = box[2 * i + 1];
+    auto q = [](float v) {
+        const float s = fminf(fmaxf(v * 1024.0f, 0.0f), 1023.0f);
+        return (uint32_t)s;
+    };
+    const uint32_t x = q(((a.x + b.x) * 0.5f - lo.x) * inv_ext.x);
+    const uint32_t y = q(((a.y + b.y) * 0.5f - lo.y) * inv_ext.y);
+    const uint32_t z = q(((a.z + b.z) * 0.5f - lo.z) * inv_ext.z);
+    keys[i] = (spread3(x) << 2) | (spread3(y) << 1) | spread3(z);
+    vals[i] = i;
+}
+
+// Longest common prefix of the keys at sorted positions i and j, with the
+// position as a tie-break; -1 outside [0, n).
+__device__ __forceinline__ int lcp(const uint32_t* __restrict__ code, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = code[i], b = code[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+// parent_* entries are (parent node << 1) | slot, -1 for the root.
+__global__ void karras_kernel(const uint32_t* __restrict__ code, const uint32_t* __restrict__ obj, int n,
+                              BvhNode* nodes, int* parent_node, int* parent_leaf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (lcp(code, n, i, i + 1) - lcp(code, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = lcp(code, n, i, i - d);
+    int lmax = 2;
+    while (lcp(code, n, i, i + lmax * d) > dmin) lmax <<= 1;  // ends: lcp is -1 past the array
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (lcp(code, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = lcp(code, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (lcp(code, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int g = i + s * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    int c0, c1;
+    if (lo == g) {
+        c0 = ~(int)obj[g];
+        parent_leaf[g] = (i << 1) | 0;
+    } else {
+        c0 = g;
+        parent_node[g] = (i << 1) | 0;
+    }
+    if (hi == g + 1) {
+        c1 = ~(int)obj[g + 1];
+        parent_leaf[g + 1] = (i << 1) | 1;
+    } else {
+        c1 = g + 1;
+        parent_node[g + 1] = (i << 1) | 1;
+    }
+    nodes[i].a.w = __int_as_float(c0);
+    nodes[i].b.w = __int_as_float(c1);
+    if (i == 0) parent_node[0] = -1;
+}
+
+__device__ __forceinline__ void put_box(BvhNode* nd, int slot, float3 lo, float3 hi) {
+    if (slot == 0) {
+        nd->a.x = lo.x; nd->a.y = lo.y; nd->a.z = lo.z;
+        nd->b.x = hi.x; nd->b.y = hi.y; nd->b.z = hi.z;
+    } else {
+        nd->c.x = lo.x; nd->c.y = lo.y; nd->c.z = lo.z;
+        nd->d.x = hi.x; nd->d.y = hi.y; nd->d.z = hi.z;
+    }
+}
+
+__global__ void refit_kernel(const float4* __restrict__ box, const uint32_t* __restrict__ obj,
+                             const int* __restrict__ parent_node, const int* __restrict__ parent_leaf, int n,
+                             BvhNode* nodes, uint32_t* flags) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 a = box[2 * obj[k]], b = box[2 * obj[k] + 1];
+    float3 lo = make_float3(a.x, a.y, a.z), hi = make_float3(b.x, b.y, b.z);
+    int p = parent_leaf[k];
+    for (int level = 0; level < 128 && p >= 0; ++level) {
+        const int node = p >> 1;
+        put_box(&nodes[node], p & 1, lo, hi);
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0u) return;  // the sibling finishes this node
+        __threadfence();
+        const float4 na = __ldcg(&nodes[node].a), nb = __ldcg(&nodes[node].b);
+        const float4 nc = __ldcg(&nodes[node].c), ndd = __ldcg(&nodes[node].d);
+        lo = make_float3(fminf(na.x, nc.x), fminf(na.y, nc.y), fminf(na.z, nc.z));
+        hi = make_float3(fmaxf(nb.x, ndd.x), fmaxf(nb.y, ndd.y), fmaxf(nb.z, ndd.z));
+        p = parent_node[node];
+    }
+}
+
+__global__ void depth_kernel(const int* __restrict__ parent_node, const int* __restrict__ parent_leaf, int n,
+                             uint32_t* max_depth) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t depth = 1;
+    int p = parent_leaf[k];
+    while (p >= 0 && depth < 200) {
+        ++depth;
+        p = parent_node[p >> 1];
+    }
+    atomicMax(max_depth, depth);
+}
+
+}  // namespace
+
+void BvhDevice::release() {
+    cudaFree(nodes);
+    cudaFree(prims);
+    cudaFree(scratch);
+    nodes = nullptr;
+    prims = nullptr;
+    scratch = nullptr;
+    scratch_bytes = 0;
+    nobj = 0;
+}
+
+cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s, uint32_t* depth_out) {
+    const uint32_t n = sc->object_count;
+    out.release();
+    if (n == 0) return cudaSuccess;
+    // Primitive records, object boxes, centre bounds, R and rmin on the host.
+    std::vector<float4> prims(2 * (size_t)n), box(2 * (size_t)n);
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float scene_r = 0.0f, rmin = INFINITY;
+    for (uint32_t i = 0; i < n; ++i) {
+        const rdc_object& o = sc->objects[i];
+        const float* c = o.center;
+        int kind = (int)o.geometry;
+        float kb;
+        std::memcpy(&kb, &kind, 4);
+        float ext;
+        if (o.geometry == RDC_GEOMETRY_SPHERE) {
+            prims[2 * i] = make_float4(c[0], c[1], c[2], (c[0] * c[0] + c[1] * c[1]) + c[2] * c[2]);
+            prims[2 * i + 1] = make_float4(o.radius * o.radius, 0.0f, 0.0f, kb);
+            ext = std::fabs(o.radius);
+            rmin = std::min(rmin, ext);
+        } else {
+            const float h = o.side_length * 0.5f;
+            prims[2 * i] = make_float4(c[0] - h, c[0] + h, c[1] - h, c[1] + h);
+            prims[2 * i + 1] = make_float4(c[2] - h, c[2] + h, 0.0f, kb);
+            ext = std::fabs(h);
+        }
+        box[2 * i] = make_float4(c[0] - ext, c[1] - ext, c[2] - ext, 0.0f);
+        box[2 * i + 1] = make_float4(c[0] + ext, c[1] + ext, c[2] + ext, 0.0f);
+        for (int a = 0; a < 3; ++a) {
+            clo[a] = std::min(clo[a], c[a]);
+            chi[a] = std::max(chi[a], c[a]);
+        }
+        const float cl = std::sqrt((c[0] * c[0] + c[1] * c[1]) + c[2] * c[2]);
+        scene_r = std::max(scene_r, cl + ext * 1.7320508f);
+    }
+    if (!(rmin < INFINITY)) rmin = 0.0f;
+    out.nobj = n;
+    out.scene_r = scene_r * 1.0001f;
+    out.rmin = rmin;
+
+    // Device buffers: nodes + prims are kept; the rest is build scratch.
+    cudaError_t e = cudaMalloc((void**)&out.prims, prims.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&out.nodes, (size_t)std::max<uint32_t>(n - 1, 1) * sizeof(BvhNode));
+    size_t sort_tmp = 0;
+    if (e == cudaSuccess)
+        e = cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                            (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30, s);
+    // scratch: box (2n float4) | keys, keys2, vals, vals2 (4n u32) | parents (2n int) | flags (n u32) | depth | sort tmp
+    const size_t box_b = 2 * (size_t)n * sizeof(float4);
+    const size_t u32_b = (size_t)n * 4;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t total = up(box_b) + 7 * up(u32_b) + up(256) + up(sort_tmp) + 256;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&out.scratch, total);
+    if (e != cudaSuccess) {
+        out.release();
+        return e;
+    }
+    out.scratch_bytes = total;
+    char* sp = static_cast<char*>(out.scratch);
+    auto take = [&](size_t bytes) {
+        char* p = sp;
+        sp += (bytes + 255) & ~(size_t)255;
+        return p;
+    };
+    float4* d_box = (float4*)take(box_b);
+    uint32_t* keys = (uint32_t*)take(u32_b);
+    uint32_t* keys2 = (uint32_t*)take(u32_b);
+    uint32_t* vals = (uint32_t*)take(u32_b);
+    uint32_t* vals2 = (uint32_t*)take(u32_b);
+    int* parent_node = (int*)take(u32_b);
+    int* parent_leaf = (int*)take(u32_b);
+    uint32_t* flags = (uint32_t*)take(u32_b);
+    uint32_t* d_depth = (uint32_t*)take(256);
+    void* d_sort = take(sort_tmp);
+
+    e = cudaMemcpyAsync(out.prims, prims.data(), prims.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_box, box.data(), box_b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, u32_b, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_depth, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(out.nodes, 0, (size_t)std::max<uint32_t>(n - 1, 1) * sizeof(BvhNode), s);
+    if (e != cudaSuccess) return e;
+    const float3 lo = make_float3(clo[0], clo[1], clo[2]);
+    auto inv = [](float a, float b) { return b > a ? 1.0f / (b - a) : 0.0f; };
+    const float3 inv_ext = make_float3(inv(clo[0], chi[0]), inv(clo[1], chi[1]), inv(clo[2], chi[2]));
+    const uint32_t B = 256, G = (n + B - 1) / B;
+    morton_kernel<<<G, B, 0, s>>>(d_box, n, lo, inv_ext, keys, vals);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = cub::DeviceRadixSort::SortPairs(d_sort, sort_tmp, keys, keys2, vals, vals2, (int)n, 0, 30, s);
+    if (e != cudaSuccess) return e;
+    if (n >= 2) {
+        karras_kernel<<<(n - 1 + B - 1) / B, B, 0, s>>>(keys2, vals2, (int)n, out.nodes, parent_node, parent_leaf);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        refit_kernel<<<G, B, 0, s>>>(d_box, vals2, parent_node, parent_leaf, (int)n, out.nodes, flags);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        depth_kernel<<<G, B, 0, s>>>(parent_node, parent_leaf, (int)n, d_depth);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    uint32_t depth = 1;
+    if (n >= 2) {
+        e = cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+    } else {
+        e = cudaStreamSynchronize(s);
+    }
+    if (depth_out) *depth_out = depth;
+    cudaFree(out.scratch);
+    out.scratch = nullptr;
+    out.scratch_bytes = 0;
+    return e;
+}
+
+}  // namespace rdc

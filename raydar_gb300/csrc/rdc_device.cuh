@@ -481,12 +481,23 @@ __device__ __forceinline__ void path_start(const SceneView& sc, uint32_t pix, Pa
     s.bounce = 0;
 }
 
+// Brute-force closest hit over a scene's records (shared or global memory).
+struct BruteIsect {
+    const float4* rec;
+    const int4* runs;
+    int nruns;
+    bool scene_fast;
+    __device__ __forceinline__ void operator()(const RayPre& r, float& t, int& idx) {
+        intersect_all(rec, runs, nruns, scene_fast, r, t, idx);
+    }
+};
+
 // One segment of a path (src/renderer/cpu.rs:256-338): trace_ray, then the
-// scatter of a hit or the world sample of a miss.  `rec`/`runs` are the
-// scene's intersection records (shared or global memory).  Returns true when
-// the path has ended (a miss, or max_bounces segments traced).
-__device__ __forceinline__ bool path_segment(const SceneView& sc, const float4* __restrict__ rec,
-                                             const int4* __restrict__ runs, PathState& s, uint32_t pix,
+// scatter of a hit or the world sample of a miss.  `isect` finds the closest
+// hit (brute force or BVH: the same result).  Returns true when the path has
+// ended (a miss, or max_bounces segments traced).
+template <class Isect>
+__device__ __forceinline__ bool path_segment(const SceneView& sc, Isect& isect, PathState& s, uint32_t pix,
                                              uint32_t sample, uint32_t max_bounces, uint32_t stream_id,
                                              uint32_t k0, uint32_t k1, uint32_t& segs) {
     if (s.bounce >= max_bounces) return true;  // max_bounces == 0: the path adds (0, 0, 0, 1)
@@ -494,7 +505,7 @@ __device__ __forceinline__ bool path_segment(const SceneView& sc, const float4* 
     const RayPre r = ray_pre(s.o, s.d, sc.neg_zero);
     float t;
     int idx;
-    intersect_all(rec, runs, (int)sc.nruns, sc.fast_div != 0u, r, t, idx);
+    isect(r, t, idx);
     if (idx < 0) {
         const V3 sky = world_sample(sc, s.d);
         s.light = vadd(s.light, mk(sky.x * s.atten.x, sky.y * s.atten.y, sky.z * s.atten.z));

@@ -51,8 +51,38 @@ struct SceneView {
     float solid[3];
 };
 
+struct BvhNode;  // rdc_bvh.cuh
+
+// Device LBVH of a scene (rdc_bvh.cu): N-1 nodes (root 0) and 2 records per
+// object in scene order.
+struct BvhView {
+    const BvhNode* nodes;
+    const float4* prims;
+    uint32_t nobj;
+    float scene_r;  // bound on |centre| + size over the objects
+    float rmin;     // smallest sphere radius (0 without spheres)
+};
+
+struct BvhDevice {
+    BvhNode* nodes = nullptr;
+    float4* prims = nullptr;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t nobj = 0;
+    float scene_r = 0.0f;
+    float rmin = 0.0f;
+    void release();
+    BvhView view() const { return BvhView{nodes, prims, nobj, scene_r, rmin}; }
+};
+
+// Build the LBVH of `sc` on stream `s` (synchronises it).  depth_out: the
+// deepest leaf (the traversal stack holds 64 entries).
+cudaError_t build_lbvh(const struct rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s, uint32_t* depth_out);
+
 struct RenderParams {
     SceneView sc;
+    BvhView bvh;                      // used by render_bvh_kernel
+    unsigned long long* bvh_counters; // [0] node visits, [1] primitive tests
     float4* accum;
     uint32_t s0;
     uint32_t nspp;
@@ -89,13 +119,16 @@ struct BatchParams {
 // Kernel launchers (rdc_kernels.cu).  Each returns the cudaError_t of its
 // launch.
 cudaError_t launch_render(const RenderParams& p, int grid, int block, size_t smem, cudaStream_t s);
+cudaError_t launch_render_bvh(const RenderParams& p, int grid, int block, cudaStream_t s);
+cudaError_t render_bvh_occupancy(int block, int* blocks_per_sm);
 cudaError_t render_occupancy(int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_batch(const BatchParams& p, int grid, int block, size_t smem, cudaStream_t s);
 cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_tonemap(const float4* accum, uint32_t npix, uint32_t sample_count, uchar4* out,
                            cudaStream_t s);
-cudaError_t launch_intersect_rays(const SceneView& sc, const float* o, const float* d, uint32_t n,
-                                  float* t, int32_t* idx, float* nrm, uint8_t* front,
+// bvh.nodes == nullptr: brute force over sc.rec; otherwise through the BVH.
+cudaError_t launch_intersect_rays(const SceneView& sc, const BvhView& bvh, const float* o, const float* d,
+                                  uint32_t n, float* t, int32_t* idx, float* nrm, uint8_t* front,
                                   cudaStream_t s);
 cudaError_t launch_scatter_fixed(const SceneView& sc, const float* o, const float* d,
                                  const float* t, const int32_t* idx, const uint32_t* words,

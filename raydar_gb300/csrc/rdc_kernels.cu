@@ -14,21 +14,16 @@
 // depend on scheduling.
 #include <cstdint>
 
+#include "rdc_bvh.cuh"
 #include "rdc_device.cuh"
 
 namespace rdc {
 
-__global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderParams P) {
-    extern __shared__ float4 smem[];
-    float4* s_rec = smem;
-    int4* s_runs = reinterpret_cast<int4*>(smem + P.sc.nrec);
-    for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
-    for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
-    __syncthreads();
-
+// The persistent per-lane loop over the pixel pool (see the file comment).
+template <class Isect>
+__device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& isect) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-
     int pix = -1;
     uint32_t sample = 0, send = 0;
     PathState st;
@@ -62,8 +57,8 @@ __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderPar
         if (__ballot_sync(FULL, pix >= 0) == 0u) break;
         if (pix < 0) continue;  // idle lane: rejoins the warp at the refill ballot
 
-        if (path_segment(P.sc, s_rec, s_runs, st, (uint32_t)pix, sample, P.max_bounces, P.stream_id, P.key0,
-                         P.key1, segs)) {
+        if (path_segment(P.sc, isect, st, (uint32_t)pix, sample, P.max_bounces, P.stream_id, P.key0, P.key1,
+                         segs)) {
             acc.x = acc.x + st.light.x;
             acc.y = acc.y + st.light.y;
             acc.z = acc.z + st.light.z;
@@ -79,12 +74,47 @@ __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderPar
             }
         }
     }
+    return segs;
+}
 
-    // Segment counter: warp sum, one 64-bit atomic per warp.
-    unsigned long long s = segs;
+__device__ __forceinline__ void add_warp_sum(unsigned long long* dst, unsigned long long v) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
-    if (lane == 0 && s != 0ull) atomicAdd(P.segments, s);
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0 && v != 0ull) atomicAdd(dst, v);
+}
+
+// Brute force: the scene's records are staged in shared memory per block.
+__global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderParams P) {
+    extern __shared__ float4 smem[];
+    float4* s_rec = smem;
+    int4* s_runs = reinterpret_cast<int4*>(smem + P.sc.nrec);
+    for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
+    for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
+    __syncthreads();
+    BruteIsect isect{s_rec, s_runs, (int)P.sc.nruns, P.sc.fast_div != 0u};
+    const uint32_t segs = render_loop(P, isect);
+    add_warp_sum(P.segments, segs);
+}
+
+// Large scenes: the closest hit through the device-built LBVH.
+struct BvhIsect {
+    BvhView bv;
+    bool scene_fast;
+    BvhCounters cnt;
+    __device__ __forceinline__ void operator()(const RayPre& r, float& t, int& idx) {
+        if (scene_fast && r.fast)
+            bvh_intersect<true>(bv, r, t, idx, cnt);
+        else
+            bvh_intersect<false>(bv, r, t, idx, cnt);
+    }
+};
+
+__global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const RenderParams P) {
+    BvhIsect isect{P.bvh, P.sc.fast_div != 0u, BvhCounters()};
+    const uint32_t segs = render_loop(P, isect);
+    add_warp_sum(P.segments, segs);
+    add_warp_sum(P.bvh_counters, isect.cnt.visits);
+    add_warp_sum(P.bvh_counters + 1, isect.cnt.tests);
 }
 
 // Many scenes in one persistent launch.  A block works on one scene at a
@@ -189,7 +219,8 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
             }
             if (__ballot_sync(FULL, pix >= 0) == 0u && !pool_open) break;
             if (pix < 0) continue;
-            if (path_segment(s_bs.sc, s_rec, s_runs, st, (uint32_t)pix, sample, s_bs.max_bounces,
+            BruteIsect isect{s_rec, s_runs, (int)s_bs.sc.nruns, s_bs.sc.fast_div != 0u};
+            if (path_segment(s_bs.sc, isect, st, (uint32_t)pix, sample, s_bs.max_bounces,
                              (uint32_t)scene, s_bs.key0, s_bs.key1, segs)) {
                 acc.x = acc.x + st.light.x;
                 acc.y = acc.y + st.light.y;
@@ -212,10 +243,7 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
         __syncthreads();
     }
 
-    unsigned long long s = segs;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
-    if (lane == 0 && s != 0ull) atomicAdd(P.segments, s);
+    add_warp_sum(P.segments, segs);
 }
 
 // print_frame_buffer, src/renderer/cpu.rs:221-230.
@@ -231,7 +259,7 @@ __global__ void tonemap_kernel(const float4* __restrict__ acc, uint32_t npix, fl
     out[i] = make_uchar4(ch(a.x), ch(a.y), ch(a.z), ch(a.w));
 }
 
-__global__ void intersect_rays_kernel(const SceneView sc, const float* __restrict__ o,
+__global__ void intersect_rays_kernel(const SceneView sc, const BvhView bvh, const float* __restrict__ o,
                                       const float* __restrict__ d, uint32_t n, float* t_out,
                                       int32_t* idx_out, float* n_out, uint8_t* f_out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -241,7 +269,12 @@ __global__ void intersect_rays_kernel(const SceneView sc, const float* __restric
     const RayPre r = ray_pre(ro, rd, sc.neg_zero);
     float t;
     int idx;
-    intersect_all(sc.rec, sc.runs, (int)sc.nruns, sc.fast_div != 0u, r, t, idx);
+    if (bvh.nodes != nullptr) {
+        BvhIsect isect{bvh, sc.fast_div != 0u, BvhCounters()};
+        isect(r, t, idx);
+    } else {
+        intersect_all(sc.rec, sc.runs, (int)sc.nruns, sc.fast_div != 0u, r, t, idx);
+    }
     idx_out[i] = idx;
     if (idx >= 0) {
         const MatDev m = sc.mat[idx];
@@ -317,6 +350,15 @@ cudaError_t launch_render(const RenderParams& p, int grid, int block, size_t sme
     return cudaGetLastError();
 }
 
+cudaError_t launch_render_bvh(const RenderParams& p, int grid, int block, cudaStream_t s) {
+    render_bvh_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t render_bvh_occupancy(int block, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, render_bvh_kernel, block, 0);
+}
+
 cudaError_t render_occupancy(int block, size_t smem, int* blocks_per_sm) {
     cudaError_t e = cudaFuncSetAttribute(render_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
@@ -343,11 +385,11 @@ cudaError_t launch_tonemap(const float4* accum, uint32_t npix, uint32_t sample_c
     return cudaGetLastError();
 }
 
-cudaError_t launch_intersect_rays(const SceneView& sc, const float* o, const float* d, uint32_t n,
-                                  float* t, int32_t* idx, float* nrm, uint8_t* front,
+cudaError_t launch_intersect_rays(const SceneView& sc, const BvhView& bvh, const float* o, const float* d,
+                                  uint32_t n, float* t, int32_t* idx, float* nrm, uint8_t* front,
                                   cudaStream_t s) {
     const uint32_t b = 128, g = (n + b - 1) / b;
-    intersect_rays_kernel<<<g, b, 0, s>>>(sc, o, d, n, t, idx, nrm, front);
+    intersect_rays_kernel<<<g, b, 0, s>>>(sc, bvh, o, d, n, t, idx, nrm, front);
     return cudaGetLastError();
 }
 

@@ -27,7 +27,9 @@ GEOMETRY_SPHERE, GEOMETRY_CUBE = 0, 1
 WORLD_SKY_COLOR, WORLD_SOLID_COLOR, WORLD_TRANSPARENT = 0, 1, 2
 PROJECTION_PERSPECTIVE, PROJECTION_ORTHOGRAPHIC = 0, 1
 MAX_RESOLUTION = 16384
-MAX_OBJECTS = 4096
+MAX_OBJECTS = 1 << 24
+MAX_BRUTE_OBJECTS = 4096
+ACCEL_AUTO, ACCEL_BRUTE_FORCE, ACCEL_LBVH = 0, 1, 2
 MAX_BOUNCES = 1024
 
 F3 = C.c_float * 3
@@ -76,6 +78,7 @@ class RdcStats(C.Structure):
         ("segments", C.c_uint64), ("paths", C.c_uint64), ("device_ms", C.c_float),
         ("sample_count", C.c_uint32), ("kernel_launches", C.c_uint32),
         ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+        ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64), ("accel", C.c_uint32), ("bvh_depth", C.c_uint32),
     ]
 
 
@@ -100,6 +103,7 @@ SIGNATURES = {
     "rdc_synchronize": (C.c_int, [_P]),
     "rdc_scene_upload": (C.c_int, [_P, C.POINTER(RdcSceneDesc)]),
     "rdc_reset": (C.c_int, [_P]),
+    "rdc_set_accel": (C.c_int, [_P, C.c_uint32]),
     "rdc_render": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
     "rdc_render_static": (C.c_int, [C.POINTER(RdcSceneDesc), C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                     C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64), C.c_char_p, C.c_size_t]),

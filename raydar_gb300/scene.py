@@ -294,3 +294,61 @@ def default_scene() -> Scene:
                Material(emission_color=np.array([0.8, 0.5, 0.2], np.float32), emission_strength=30.0)),
     ]
     return Scene(cam, World(), objs)
+
+
+# Packed rdc_object records (68 bytes, the C layout) for large generated scenes.
+OBJECT_DTYPE = np.dtype([
+    ("geometry", "<u4"), ("center", "<f4", 3), ("radius", "<f4"), ("side_length", "<f4"),
+    ("albedo", "<f4", 3), ("roughness", "<f4"), ("metallic", "<f4"), ("emission_color", "<f4", 3),
+    ("emission_strength", "<f4"), ("transmission", "<f4"), ("ior", "<f4"),
+])
+assert OBJECT_DTYPE.itemsize == C.sizeof(native.RdcObject)
+
+
+class PackedScene(Scene):
+    """A Scene whose objects live in one numpy array of OBJECT_DTYPE records
+    (generated scenes with 10^5 objects); `objects` is built lazily."""
+
+    def __init__(self, camera: Camera, world: World, packed: np.ndarray):
+        self.camera = camera
+        self.world = world
+        self.packed = packed
+        self._objects = None
+
+    @property
+    def objects(self):
+        if self._objects is None:
+            out = []
+            for r in self.packed:
+                geo = "Sphere" if r["geometry"] == native.GEOMETRY_SPHERE else "Cube"
+                size = float(r["radius"] if geo == "Sphere" else r["side_length"])
+                m = Material(r["albedo"].copy(), float(r["roughness"]), float(r["metallic"]),
+                             r["emission_color"].copy(), float(r["emission_strength"]),
+                             float(r["transmission"]), float(r["ior"]))
+                out.append(Object(geo, r["center"].copy(), size, m))
+            self._objects = out
+        return self._objects
+
+    @objects.setter
+    def objects(self, value):
+        self._objects = value
+
+    def to_c(self) -> "SceneC":
+        return PackedSceneC(self)
+
+
+class PackedSceneC(SceneC):
+    def __init__(self, scene: PackedScene):
+        n = len(scene.packed)
+        self.objects = (native.RdcObject * max(n, 1))()
+        C.memmove(self.objects, np.ascontiguousarray(scene.packed).ctypes.data, n * OBJECT_DTYPE.itemsize)
+        self.desc = native.RdcSceneDesc()
+        self.desc.camera = scene.camera.to_c()
+        w = scene.world
+        self.desc.world.kind = {"SkyColor": native.WORLD_SKY_COLOR, "SolidColor": native.WORLD_SOLID_COLOR,
+                                "Transparent": native.WORLD_TRANSPARENT}[w.kind]
+        self.desc.world.top_color[:] = [float(x) for x in w.top_color]
+        self.desc.world.bottom_color[:] = [float(x) for x in w.bottom_color]
+        self.desc.world.solid_color[:] = [float(x) for x in w.color]
+        self.desc.objects = C.cast(self.objects, C.POINTER(native.RdcObject))
+        self.desc.object_count = n

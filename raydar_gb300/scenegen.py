@@ -166,3 +166,36 @@ def c4_diff(seed: int = 4, width: int = 512, height: int = 512) -> Workload:
 
 
 WORKLOADS = {"c1_plain": c1_plain, "c2_default": c2_default, "c4_diff": c4_diff}
+
+
+def _packed_materials(rng, rec, kinds):
+    """Fill the material fields of packed records for class letters D/M/G/S."""
+    n = len(rec)
+    rec["albedo"] = rng.uniform(0.1, 0.9, (n, 3)).astype(np.float32)
+    rec["ior"] = 1.5
+    rec["roughness"] = np.where(kinds == "D", 1.0, np.where(kinds == "S", 0.5, 0.0)).astype(np.float32)
+    metal = kinds == "M"
+    rec["roughness"][metal] = rng.uniform(0.0, 0.5, metal.sum()).astype(np.float32)
+    rec["metallic"] = metal.astype(np.float32)
+    rec["transmission"] = (kinds == "G").astype(np.float32)
+
+
+def c5_large(seed: int = 5, width: int = 1920, height: int = 1080, n_spheres: int = 100_000,
+             n_cubes: int = 10_000) -> Workload:
+    """100k spheres (radius log-uniform in [0.01, 0.2]) and 10k cubes (edge
+    U[0.02, 0.3]) with centres uniform in a 40 x 10 x 40 box, the usual
+    material mix; 1920x1080, 256 spp, 12 bounces (device-built LBVH)."""
+    from .scene import OBJECT_DTYPE, PackedScene
+    rng = np.random.default_rng(seed)
+    n = n_spheres + n_cubes
+    rec = np.zeros(n, OBJECT_DTYPE)
+    rec["geometry"][:n_spheres] = 0
+    rec["geometry"][n_spheres:] = 1
+    rec["center"] = np.stack([rng.uniform(-20, 20, n), rng.uniform(0, 10, n), rng.uniform(-20, 20, n)], 1)
+    rec["radius"][:n_spheres] = np.exp(rng.uniform(np.log(0.01), np.log(0.2), n_spheres))
+    rec["side_length"][n_spheres:] = rng.uniform(0.02, 0.3, n_cubes)
+    kinds = np.array(_mix_kinds(rng, n))
+    _packed_materials(rng, rec, kinds)
+    cam = _camera(width, height, [0.0, 6.0, -32.0], [0.0, 5.0, 0.0], 50.0)
+    sky = World("SkyColor", np.array(SKY_TOP, np.float32), np.array(SKY_BOTTOM, np.float32))
+    return Workload("c5_large", PackedScene(cam, sky, rec), 256, 12)

@@ -227,7 +227,7 @@ def test_scene_errors(renderer):
     assert b"Transparent" in lib.rdc_last_error(ctx)
     scene.world.kind = "SkyColor"
     sc = scene.to_c()
-    sc.desc.object_count = 5000
+    sc.desc.object_count = native.MAX_OBJECTS + 1
     assert lib.rdc_scene_upload(ctx, sc.ref()) == 3  # RDC_ERR_LIMIT
     sc = scene.to_c()
     sc.desc.camera.resolution_x = 0
