@@ -279,6 +279,14 @@ rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config);
  * Leaves the accumulators of the last trial; render again for results. */
 rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* best_ms_out);
 
+/* Set / get the launch shape of rdc_render.  block_size and blocks_per_sm as
+ * for a batch (default 256, 0).  refill_min_idle applies to LBVH renders: a
+ * warp keeps stepping its lanes' traversals until this many have finished,
+ * then shades those together (default 16).  Brute-force renders refill each
+ * idle lane at once.  Affects results never, speed only. */
+rdc_status rdc_set_render_config(rdc_ctx* ctx, const rdc_launch_config* config);
+rdc_status rdc_get_render_config(rdc_ctx* ctx, rdc_launch_config* config);
+
 /* ---- fixed-input entry points (parity checks of single stages) -------- */
 
 /* Closest hit of n rays against the uploaded scene: Ray::hit / trace_ray /

@@ -51,7 +51,7 @@ struct rdc_ctx {
     uint64_t last_paths = 0;
     bool last_timed = false;
     uint32_t last_launches = 0;
-    int render_block = rdc::kRenderBlock;
+    rdc_launch_config render_cfg{(uint32_t)rdc::kRenderBlock, 0, 16};
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
     // closest-hit acceleration
@@ -423,23 +423,26 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
                     "RDC_MAX_BRUTE_OBJECTS objects); use RDC_ACCEL_LBVH or RDC_ACCEL_AUTO");
     p.bvh = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
     p.bvh_counters = ctx->d_counters + 2;
+    p.min_idle = ctx->render_cfg.refill_min_idle;
+    const int block = (int)ctx->render_cfg.block_size;
     const size_t smem = ctx->bvh_active ? 0 : rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
     int per_sm = 0;
     if (ctx->bvh_active)
-        RDC_CUDA(ctx, rdc::render_bvh_occupancy(ctx->render_block, &per_sm));
+        RDC_CUDA(ctx, rdc::render_bvh_occupancy(block, &per_sm));
     else
-        RDC_CUDA(ctx, rdc::render_occupancy(ctx->render_block, smem, &per_sm));
+        RDC_CUDA(ctx, rdc::render_occupancy(block, smem, &per_sm));
     if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: scene does not fit in shared memory");
+    if (ctx->render_cfg.blocks_per_sm != 0) per_sm = std::min<int>(per_sm, (int)ctx->render_cfg.blocks_per_sm);
     const uint64_t warps_needed = ((uint64_t)p.npix + 31) / 32;
     uint64_t grid = (uint64_t)ctx->num_sms * per_sm;
-    const uint64_t grid_needed = (warps_needed * 32 + ctx->render_block - 1) / ctx->render_block;
+    const uint64_t grid_needed = (warps_needed * 32 + block - 1) / block;
     if (grid > grid_needed) grid = grid_needed;
 
     RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     if (ctx->bvh_active)
-        RDC_CUDA(ctx, rdc::launch_render_bvh(p, (int)grid, ctx->render_block, ctx->stream));
+        RDC_CUDA(ctx, rdc::launch_render_bvh(p, (int)grid, block, ctx->stream));
     else
-        RDC_CUDA(ctx, rdc::launch_render(p, (int)grid, ctx->render_block, smem, ctx->stream));
+        RDC_CUDA(ctx, rdc::launch_render(p, (int)grid, block, smem, ctx->stream));
     RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->last_timed = true;
     ctx->last_launches = 1;
@@ -823,6 +826,23 @@ rdc_status rdc_batch_set_config(rdc_ctx* ctx, const rdc_launch_config* config) {
     if (ctx->batch.n == 0) return RDC_OK;
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return capture_batch_graph(ctx);
+}
+
+rdc_status rdc_set_render_config(rdc_ctx* ctx, const rdc_launch_config* config) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!config) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_set_render_config: NULL config");
+    if (config->block_size != 64 && config->block_size != 128 && config->block_size != 256)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_set_render_config: block_size must be 64, 128 or 256");
+    if (config->refill_min_idle < 1 || config->refill_min_idle > 32)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_set_render_config: refill_min_idle must be in 1..32");
+    ctx->render_cfg = *config;
+    return RDC_OK;
+}
+
+rdc_status rdc_get_render_config(rdc_ctx* ctx, rdc_launch_config* config) {
+    if (!ctx || !config) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_get_render_config: NULL argument");
+    *config = ctx->render_cfg;
+    return RDC_OK;
 }
 
 rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config) {

@@ -165,41 +165,69 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     const uint32_t n = sc->object_count;
     out.release();
     if (n == 0) return cudaSuccess;
-    // Primitive records, object boxes, centre bounds, R and rmin on the host.
+    // Primitive records, object boxes, centre bounds and R on the host.
     std::vector<float4> prims(2 * (size_t)n), box(2 * (size_t)n);
     float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    float scene_r = 0.0f, rmin = INFINITY;
+    double scene_r = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const rdc_object& o = sc->objects[i];
+        const double ext = o.geometry == RDC_GEOMETRY_SPHERE ? std::fabs((double)o.radius)
+                                                               : std::fabs((double)o.side_length) * 0.5;
+        double cl = 0.0;
+        for (int a = 0; a < 3; ++a) cl += (double)o.center[a] * (double)o.center[a];
+        scene_r = std::max(scene_r, std::sqrt(cl) + ext * 1.7320508075688772);
+    }
+    // Sphere leaf boxes are grown for origins up to o_max: the camera (its
+    // primary rays) or any point of the scene (the hit points that start
+    // every later segment).  Rays from further away add the rest per ray.
+    const double cam = std::sqrt((double)sc->camera.position[0] * sc->camera.position[0] +
+                                 (double)sc->camera.position[1] * sc->camera.position[1] +
+                                 (double)sc->camera.position[2] * sc->camera.position[2]);
+    const double o_max = std::max(cam, scene_r * 1.0001);
+    // float lower / upper neighbours of a double (outward rounding)
+    auto down = [](double x) {
+        float f = (float)x;
+        if ((double)f > x) f = std::nextafter(f, -INFINITY);
+        return f;
+    };
+    auto upr = [](double x) {
+        float f = (float)x;
+        if ((double)f < x) f = std::nextafter(f, INFINITY);
+        return f;
+    };
     for (uint32_t i = 0; i < n; ++i) {
         const rdc_object& o = sc->objects[i];
         const float* c = o.center;
         int kind = (int)o.geometry;
         float kb;
         std::memcpy(&kb, &kind, 4);
-        float ext;
+        double ext;
         if (o.geometry == RDC_GEOMETRY_SPHERE) {
             prims[2 * i] = make_float4(c[0], c[1], c[2], (c[0] * c[0] + c[1] * c[1]) + c[2] * c[2]);
             prims[2 * i + 1] = make_float4(o.radius * o.radius, 0.0f, 0.0f, kb);
-            ext = std::fabs(o.radius);
-            rmin = std::min(rmin, ext);
+            // The expanded quadratic can report a hit for a ray passing within
+            // sqrt(r^2 (1 + 2^-20) + 2^-19 (|o| + |c|)^2) of the centre (the
+            // rounding bound in the traversal's comment).
+            const double r = std::fabs((double)o.radius);
+            const double cn = std::sqrt(((double)c[0] * c[0] + (double)c[1] * c[1]) + (double)c[2] * c[2]);
+            const double s = o_max + cn;
+            ext = std::sqrt(r * r * (1.0 + 0x1p-20) + 0x1p-19 * s * s) * (1.0 + 0x1p-40);
         } else {
             const float h = o.side_length * 0.5f;
             prims[2 * i] = make_float4(c[0] - h, c[0] + h, c[1] - h, c[1] + h);
             prims[2 * i + 1] = make_float4(c[2] - h, c[2] + h, 0.0f, kb);
-            ext = std::fabs(h);
+            ext = std::fabs((double)h);
         }
-        box[2 * i] = make_float4(c[0] - ext, c[1] - ext, c[2] - ext, 0.0f);
-        box[2 * i + 1] = make_float4(c[0] + ext, c[1] + ext, c[2] + ext, 0.0f);
+        box[2 * i] = make_float4(down(c[0] - ext), down(c[1] - ext), down(c[2] - ext), 0.0f);
+        box[2 * i + 1] = make_float4(upr(c[0] + ext), upr(c[1] + ext), upr(c[2] + ext), 0.0f);
         for (int a = 0; a < 3; ++a) {
             clo[a] = std::min(clo[a], c[a]);
             chi[a] = std::max(chi[a], c[a]);
         }
-        const float cl = std::sqrt((c[0] * c[0] + c[1] * c[1]) + c[2] * c[2]);
-        scene_r = std::max(scene_r, cl + ext * 1.7320508f);
     }
-    if (!(rmin < INFINITY)) rmin = 0.0f;
     out.nobj = n;
-    out.scene_r = scene_r * 1.0001f;
-    out.rmin = rmin;
+    out.scene_r = upr(scene_r * 1.0001);
+    out.o_max = down(o_max);
 
     // Device buffers: nodes + prims are kept; the rest is build scratch.
     cudaError_t e = cudaMalloc((void**)&out.prims, prims.size() * sizeof(float4));

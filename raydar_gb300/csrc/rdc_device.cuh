@@ -492,20 +492,16 @@ struct BruteIsect {
     }
 };
 
-// One segment of a path (src/renderer/cpu.rs:256-338): trace_ray, then the
-// scatter of a hit or the world sample of a miss.  `isect` finds the closest
-// hit (brute force or BVH: the same result).  Returns true when the path has
-// ended (a miss, or max_bounces segments traced).
-template <class Isect>
-__device__ __forceinline__ bool path_segment(const SceneView& sc, Isect& isect, PathState& s, uint32_t pix,
-                                             uint32_t sample, uint32_t max_bounces, uint32_t stream_id,
-                                             uint32_t k0, uint32_t k1, uint32_t& segs) {
-    if (s.bounce >= max_bounces) return true;  // max_bounces == 0: the path adds (0, 0, 0, 1)
-    ++segs;
-    const RayPre r = ray_pre(s.o, s.d, sc.neg_zero);
-    float t;
-    int idx;
-    isect(r, t, idx);
+// path_segment (below) runs one segment of a path (src/renderer/cpu.rs:256-338):
+// trace_ray, then the scatter of a hit or the world sample of a miss.  `isect`
+// finds the closest hit (brute force or BVH: the same result).  It returns
+// true when the path has ended (a miss, or max_bounces segments traced).
+//
+// segment_shade is its second half: given the closest hit (t, idx; idx < 0
+// for none) of the ray (s.o, s.d), apply the world sample or the scatter.
+__device__ __forceinline__ bool segment_shade(const SceneView& sc, PathState& s, float t, int idx, uint32_t pix,
+                                              uint32_t sample, uint32_t max_bounces, uint32_t stream_id,
+                                              uint32_t k0, uint32_t k1) {
     if (idx < 0) {
         const V3 sky = world_sample(sc, s.d);
         s.light = vadd(s.light, mk(sky.x * s.atten.x, sky.y * s.atten.y, sky.z * s.atten.z));
@@ -530,6 +526,19 @@ __device__ __forceinline__ bool path_segment(const SceneView& sc, Isect& isect, 
     s.light = vadd(s.light, mk(m.b.x, m.b.y, m.b.z));
     ++s.bounce;
     return s.bounce >= max_bounces;
+}
+
+template <class Isect>
+__device__ __forceinline__ bool path_segment(const SceneView& sc, Isect& isect, PathState& s, uint32_t pix,
+                                             uint32_t sample, uint32_t max_bounces, uint32_t stream_id,
+                                             uint32_t k0, uint32_t k1, uint32_t& segs) {
+    if (s.bounce >= max_bounces) return true;  // max_bounces == 0: the path adds (0, 0, 0, 1)
+    ++segs;
+    const RayPre r = ray_pre(s.o, s.d, sc.neg_zero);
+    float t;
+    int idx;
+    isect(r, t, idx);
+    return segment_shade(sc, s, t, idx, pix, sample, max_bounces, stream_id, k0, k1);
 }
 
 }  // namespace rdc

@@ -60,7 +60,7 @@ struct BvhView {
     const float4* prims;
     uint32_t nobj;
     float scene_r;  // bound on |centre| + size over the objects
-    float rmin;     // smallest sphere radius (0 without spheres)
+    float o_max;    // sphere leaf boxes are grown for ray origins with |o| <= o_max
 };
 
 struct BvhDevice {
@@ -70,9 +70,9 @@ struct BvhDevice {
     size_t scratch_bytes = 0;
     uint32_t nobj = 0;
     float scene_r = 0.0f;
-    float rmin = 0.0f;
+    float o_max = 0.0f;
     void release();
-    BvhView view() const { return BvhView{nodes, prims, nobj, scene_r, rmin}; }
+    BvhView view() const { return BvhView{nodes, prims, nobj, scene_r, o_max}; }
 };
 
 // Build the LBVH of `sc` on stream `s` (synchronises it).  depth_out: the
@@ -93,6 +93,7 @@ struct RenderParams {
     uint32_t npix;
     uint32_t* work_counter;
     unsigned long long* segments;
+    uint32_t min_idle;                // render_bvh_kernel: lanes done before a warp shades
 };
 
 // One scene of a batch (rdc_batch_upload): its view, accumulator, sample

@@ -102,19 +102,118 @@ struct BvhIsect {
     bool scene_fast;
     BvhCounters cnt;
     __device__ __forceinline__ void operator()(const RayPre& r, float& t, int& idx) {
-        if (scene_fast && r.fast)
-            bvh_intersect<true>(bv, r, t, idx, cnt);
-        else
-            bvh_intersect<false>(bv, r, t, idx, cnt);
+        bvh_intersect(bv, r, scene_fast && r.fast, t, idx, cnt);
     }
 };
 
+// The LBVH kernel keeps render_kernel's pixel ownership (a pixel's samples
+// run back to back on one lane, so accumulation order is the reference's)
+// but loops over node visits instead of segments: ray lengths through the
+// tree differ by an order of magnitude, and a warp that ran one whole
+// traversal per lane per iteration would wait for its slowest ray.  Each
+// iteration takes traversal steps while fewer than `min_idle` lanes have
+// finished theirs, then the finished lanes shade together (scatter or world
+// sample), start their next segment, sample or pixel, and traversal resumes.
 __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const RenderParams P) {
-    BvhIsect isect{P.bvh, P.sc.fast_div != 0u, BvhCounters()};
-    const uint32_t segs = render_loop(P, isect);
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool scene_fast = P.sc.fast_div != 0u;
+    int stack_node[kBvhStack];
+    float stack_entry[kBvhStack];
+    BvhCounters cnt;
+    BvhTrav T;
+    T.cur = -1;
+    T.best = 0.0f;
+    T.bidx = -1;
+    RayPre r;
+    bool rfast = false;
+    int pix = -1;
+    uint32_t sample = 0, send = 0;
+    PathState st;
+    st.o = st.d = st.atten = st.light = mk(0.f, 0.f, 0.f);
+    st.bounce = 0;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t segs = 0;
+    bool pool_open = true;
+    bool in_flight = false;  // a segment of this lane's path is being traced
+
+    // Close finished paths and start the next segment of this lane's pixel
+    // (ended: the current path is over).  Leaves in_flight with a running
+    // traversal, or pix = -1 when the pixel's samples are all done.
+    auto advance = [&](bool ended) {
+        for (;;) {
+            if (ended) {
+                acc.x = acc.x + st.light.x;
+                acc.y = acc.y + st.light.y;
+                acc.z = acc.z + st.light.z;
+                acc.w = acc.w + 1.0f;
+                ++sample;
+                if (sample == send) {
+                    P.accum[pix] = acc;
+                    pix = -1;
+                    in_flight = false;
+                    return;
+                }
+                path_start(P.sc, (uint32_t)pix, st);
+            }
+            if (st.bounce >= P.max_bounces) {  // max_bounces == 0: the path adds (0, 0, 0, 1)
+                ended = true;
+                continue;
+            }
+            ++segs;
+            r = ray_pre(st.o, st.d, P.sc.neg_zero);
+            rfast = scene_fast && r.fast;
+            bvh_begin(P.bvh, r, rfast, T, cnt);
+            if (T.cur >= 0) {
+                in_flight = true;
+                return;
+            }
+            ended = segment_shade(P.sc, st, T.best, T.bidx, (uint32_t)pix, sample, P.max_bounces, P.stream_id,
+                                  P.key0, P.key1);
+        }
+    };
+
+    for (;;) {
+        // Shade the lanes whose traversal is over and start their next segment.
+        if (in_flight && T.cur < 0) {
+            const bool ended = segment_shade(P.sc, st, T.best, T.bidx, (uint32_t)pix, sample, P.max_bounces,
+                                             P.stream_id, P.key0, P.key1);
+            advance(ended);
+        }
+        // Refill idle lanes with new pixels (warp-aggregated atomic).
+        const unsigned need = __ballot_sync(FULL, pix < 0);
+        if (need != 0u && pool_open) {
+            const unsigned cnt_need = __popc(need);
+            const int leader = __ffs(need) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(P.work_counter, cnt_need);
+            base = __shfl_sync(FULL, base, leader);
+            if (base + cnt_need >= P.npix) pool_open = false;
+            if (pix < 0) {
+                const unsigned mine = base + __popc(need & ((1u << lane) - 1u));
+                if (mine < P.npix) {
+                    pix = (int)mine;
+                    acc = P.accum[pix];
+                    path_start(P.sc, mine, st);
+                    sample = P.s0;
+                    send = P.s0 + P.nspp;
+                    advance(false);
+                }
+            }
+        }
+        if (__ballot_sync(FULL, pix >= 0) == 0u) break;
+        // Traversal steps until min_idle lanes are done (or all of them).
+        for (;;) {
+            const bool run = in_flight && T.cur >= 0;
+            const unsigned act = __ballot_sync(FULL, run);
+            if (act == 0u) break;
+            if (run) bvh_step(P.bvh, r, rfast, T, stack_node, stack_entry, cnt);
+            if (32u - (unsigned)__popc(__ballot_sync(FULL, in_flight && T.cur >= 0)) >= P.min_idle) break;
+        }
+    }
     add_warp_sum(P.segments, segs);
-    add_warp_sum(P.bvh_counters, isect.cnt.visits);
-    add_warp_sum(P.bvh_counters + 1, isect.cnt.tests);
+    add_warp_sum(P.bvh_counters, cnt.visits);
+    add_warp_sum(P.bvh_counters + 1, cnt.tests);
 }
 
 // Many scenes in one persistent launch.  A block works on one scene at a

@@ -215,6 +215,7 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
         p.npix = cam.resolution_x * cam.resolution_y;
         p.work_counter = reinterpret_cast<uint32_t*>(d_counters);
         p.segments = d_counters + 1;
+        p.min_idle = 1;
 
         const size_t smem = rdc::render_smem_bytes(fc.nrec, fc.nruns);
         int per_sm = 0;
