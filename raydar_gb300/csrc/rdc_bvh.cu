@@ -9,8 +9,11 @@
 //   5. bottom-up refit: each leaf walks towards the root; at every node the
 //      first arriving child records its box and stops (one atomic per node),
 //      the second computes the union and continues.  No thread ever waits.
-//   6. tree depth (must stay <= 64 for the traversal stack; Karras trees over
-//      30-bit codes with position tie-breaks are at most 62 deep).
+//   6. tree depth (Karras trees over 30-bit codes with position tie-breaks
+//      are at most 63 deep)
+//   7. collapse to 4-wide nodes: the binary nodes at even depth, compacted
+//      by a prefix sum (CUB), each taking its grandchildren (or its leaf
+//      children) as children.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -18,6 +21,7 @@
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "raydar_cuda.h"
 #include "rdc_bvh.cuh"
@@ -148,6 +152,55 @@ __global__ void depth_kernel(const int* __restrict__ parent_node, const int* __r
     atomicMax(max_depth, depth);
 }
 
+// even[i] = 1 when internal node i is at even depth (the root is at 0):
+// those nodes become the 4-wide tree.
+__global__ void even_depth_kernel(const int* __restrict__ parent_node, int n_internal, uint32_t* even) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal) return;
+    uint32_t depth = 0;
+    int p = parent_node[i];
+    while (p >= 0 && depth < 200) {
+        ++depth;
+        p = parent_node[p >> 1];
+    }
+    even[i] = (depth & 1u) ? 0u : 1u;
+}
+
+__device__ __forceinline__ void put4(Bvh4Node& q, int j, float4 lo, float4 hi, int child) {
+    q.v[2 * j] = make_float4(lo.x, lo.y, lo.z, __int_as_float(child));
+    q.v[2 * j + 1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+}
+
+// The 4-wide node of even-depth binary node i: its leaf children and the
+// children of its internal children (all at even depth again), at the
+// compacted index map[i] (exclusive prefix sum of even[]).
+__global__ void collapse4_kernel(const BvhNode* __restrict__ bin, const uint32_t* __restrict__ even,
+                                 const uint32_t* __restrict__ map, int n_internal, Bvh4Node* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal || !even[i]) return;
+    Bvh4Node q;
+    int k = 0;
+    const BvhNode nd = bin[i];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const int c = __float_as_int(s ? nd.b.w : nd.a.w);
+        if (c < 0) {
+            put4(q, k++, s ? nd.c : nd.a, s ? nd.d : nd.b, c);
+        } else {
+            const BvhNode m = bin[c];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const int g = __float_as_int(t ? m.b.w : m.a.w);
+                put4(q, k++, t ? m.c : m.a, t ? m.d : m.b, g < 0 ? g : (int)map[g]);
+            }
+        }
+    }
+    const float INF = __int_as_float(0x7f800000);
+    const float4 empty = make_float4(INF, INF, INF, 0.0f);
+    for (; k < 4; ++k) put4(q, k, empty, empty, 0);
+    out[map[i]] = q;
+}
+
 }  // namespace
 
 void BvhDevice::release() {
@@ -155,6 +208,7 @@ void BvhDevice::release() {
     cudaFree(prims);
     cudaFree(scratch);
     nodes = nullptr;
+    nnodes = 0;
     prims = nullptr;
     scratch = nullptr;
     scratch_bytes = 0;
@@ -229,18 +283,23 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     out.scene_r = upr(scene_r * 1.0001);
     out.o_max = down(o_max);
 
-    // Device buffers: nodes + prims are kept; the rest is build scratch.
+    // Device buffers: the 4-wide nodes + prims are kept; the rest (binary
+    // nodes included) is build scratch.
+    const size_t n_int = n >= 2 ? (size_t)n - 1 : 1;
     cudaError_t e = cudaMalloc((void**)&out.prims, prims.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&out.nodes, (size_t)std::max<uint32_t>(n - 1, 1) * sizeof(BvhNode));
-    size_t sort_tmp = 0;
+    size_t sort_tmp = 0, scan_tmp = 0;
     if (e == cudaSuccess)
         e = cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr,
                                             (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30, s);
-    // scratch: box (2n float4) | keys, keys2, vals, vals2 (4n u32) | parents (2n int) | flags (n u32) | depth | sort tmp
+    if (e == cudaSuccess)
+        e = cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n_int, s);
+    // scratch: box (2n float4) | binary nodes (n-1) | keys, keys2, vals, vals2 (4n u32) | parents (2n int) |
+    //          flags, even, map (3n u32) | depth | sort tmp | scan tmp
     const size_t box_b = 2 * (size_t)n * sizeof(float4);
+    const size_t bin_b = n_int * sizeof(BvhNode);
     const size_t u32_b = (size_t)n * 4;
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t total = up(box_b) + 7 * up(u32_b) + up(256) + up(sort_tmp) + 256;
+    const size_t total = up(box_b) + up(bin_b) + 9 * up(u32_b) + up(256) + up(sort_tmp) + up(scan_tmp) + 256;
     if (e == cudaSuccess) e = cudaMalloc((void**)&out.scratch, total);
     if (e != cudaSuccess) {
         out.release();
@@ -254,6 +313,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
         return p;
     };
     float4* d_box = (float4*)take(box_b);
+    BvhNode* bin = (BvhNode*)take(bin_b);
     uint32_t* keys = (uint32_t*)take(u32_b);
     uint32_t* keys2 = (uint32_t*)take(u32_b);
     uint32_t* vals = (uint32_t*)take(u32_b);
@@ -261,14 +321,17 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     int* parent_node = (int*)take(u32_b);
     int* parent_leaf = (int*)take(u32_b);
     uint32_t* flags = (uint32_t*)take(u32_b);
+    uint32_t* even = (uint32_t*)take(u32_b);
+    uint32_t* map = (uint32_t*)take(u32_b);
     uint32_t* d_depth = (uint32_t*)take(256);
     void* d_sort = take(sort_tmp);
+    void* d_scan = take(scan_tmp);
 
     e = cudaMemcpyAsync(out.prims, prims.data(), prims.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_box, box.data(), box_b, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, u32_b, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_depth, 0, 4, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(out.nodes, 0, (size_t)std::max<uint32_t>(n - 1, 1) * sizeof(BvhNode), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bin, 0, bin_b, s);
     if (e != cudaSuccess) return e;
     const float3 lo = make_float3(clo[0], clo[1], clo[2]);
     auto inv = [](float a, float b) { return b > a ? 1.0f / (b - a) : 0.0f; };
@@ -278,22 +341,33 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     e = cub::DeviceRadixSort::SortPairs(d_sort, sort_tmp, keys, keys2, vals, vals2, (int)n, 0, 30, s);
     if (e != cudaSuccess) return e;
+    uint32_t depth = 1;
     if (n >= 2) {
-        karras_kernel<<<(n - 1 + B - 1) / B, B, 0, s>>>(keys2, vals2, (int)n, out.nodes, parent_node, parent_leaf);
+        const uint32_t GI = (uint32_t)((n_int + B - 1) / B);
+        karras_kernel<<<GI, B, 0, s>>>(keys2, vals2, (int)n, bin, parent_node, parent_leaf);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        refit_kernel<<<G, B, 0, s>>>(d_box, vals2, parent_node, parent_leaf, (int)n, out.nodes, flags);
+        refit_kernel<<<G, B, 0, s>>>(d_box, vals2, parent_node, parent_leaf, (int)n, bin, flags);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         depth_kernel<<<G, B, 0, s>>>(parent_node, parent_leaf, (int)n, d_depth);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
-    uint32_t depth = 1;
-    if (n >= 2) {
+        even_depth_kernel<<<GI, B, 0, s>>>(parent_node, (int)n_int, even);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, even, map, (int)n_int, s);
+        if (e != cudaSuccess) return e;
+        uint32_t tail[2] = {0, 0};
         e = cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[0], map + n_int - 1, 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[1], even + n_int - 1, 4, cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
-    } else {
-        e = cudaStreamSynchronize(s);
+        out.nnodes = tail[0] + tail[1];
+        e = cudaMalloc((void**)&out.nodes, (size_t)out.nnodes * sizeof(Bvh4Node));
+        if (e != cudaSuccess) return e;
+        collapse4_kernel<<<GI, B, 0, s>>>(bin, even, map, (int)n_int, out.nodes);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
     if (depth_out) *depth_out = depth;
     cudaFree(out.scratch);
     out.scratch = nullptr;

@@ -2,8 +2,11 @@
 //
 // The reference tests every object (src/renderer/cpu.rs:344-352).  For large
 // scenes the kernels instead walk a linear BVH: Morton-ordered objects, a
-// Karras (2012) radix tree of N-1 internal nodes, each node holding the boxes
-// of its two children.  The result must be the reference's exactly:
+// Karras (2012) radix tree of N-1 internal nodes, collapsed into a 4-wide
+// tree (every binary node at even depth keeps its grandchildren, or its leaf
+// children, as up to four children): half the dependent node loads per ray,
+// four independent box tests per load.  The result must be the reference's
+// exactly:
 //   - leaves run the same exact sphere / cube tests as the brute-force loop;
 //   - the first-minimum rule (lowest object index among equal t) becomes a
 //     lexicographic minimum over (t, index), independent of visiting order;
@@ -18,11 +21,12 @@
 //     reported only when rho^2 <= r^2 (1 + 2^-20) + 2^-19 S^2.  Sphere leaf
 //     boxes are built with that radius for |o| <= o_max (rdc_bvh.cu); a ray
 //     from further away adds 2^-9.5 (|o| - o_max), the slope of that radius
-//     in S.  Every ray also adds 2^-20 (|o| + 2R), R bounding |centre| + size:
-//     it covers the computed t lying before the grown ball's entry (at most
-//     ~5u S along the ray) and the slab test's rounding for cubes
-//     (2u (|o| + |c| + h) per axis).  The per-ray growth is folded into two
-//     origin offsets, so it costs nothing per box.
+//     in S.  Every ray also adds 2^-20 (|o| + 2R) = 16u (|o| + 2R), R bounding
+//     |centre| + size: it covers the computed t lying before the grown ball's
+//     entry (at most ~5u S along the ray), the reference slab test's rounding
+//     for cubes (2u (|o| + |c| + h) per axis) and the box test's own
+//     (4u |o| + 2u |lo|), 11u |o| + 13u R in all.  The per-ray growth is
+//     folded into the two per-axis origin terms, so it costs nothing per box.
 #pragma once
 
 #include "raydar_cuda.h"
@@ -30,6 +34,7 @@
 
 namespace rdc {
 
+// Binary node of the build (rdc_bvh.cu).
 struct alignas(16) BvhNode {
     float4 a;  // child 0 box min (xyz), child 0 (int bits: >= 0 node, < 0 leaf ~object)
     float4 b;  // child 0 box max (xyz), child 1 (int bits)
@@ -37,7 +42,14 @@ struct alignas(16) BvhNode {
     float4 d;  // child 1 box max (xyz), 0
 };
 
-// BvhView (rdc_internal.hpp): nodes (N-1, root 0), prims (2 per object, scene
+// 4-wide node, 128 bytes: child j's box in v[2j] (min xyz, child in w as
+// int bits: >= 0 node, < 0 leaf ~object) and v[2j+1] (max xyz).  An unused
+// slot has min = max = +inf, which no ray hits (1/d is never 0).
+struct alignas(16) Bvh4Node {
+    float4 v[8];
+};
+
+// BvhView (rdc_internal.hpp): nodes (root 0), prims (2 per object, scene
 // order: sphere (c, c.c) (r*r, 0, 0, kind); cube in the slab pair layout with
 // kind in the last word), scene_r and o_max for the per-ray box growth.
 
@@ -92,31 +104,35 @@ __device__ __forceinline__ void bvh_leaf(const BvhView& bv, const RayPre& r, int
     }
 }
 
-// Conservative slab test of a box [lo - m, hi + m]: oa = o + m, ob = o - m.
+// Conservative slab test of a box [lo - m, hi + m] (m the per-ray growth):
+// with oa = (o + m) / d and ob = (o - m) / d per axis, the plane distances
+// are lo / d - oa and hi / d - ob, one FMA each.  Their rounding (a few ulp
+// of |o| + |lo| along the ray) is far inside the 2^-20 (|o| + 2R) part of m,
+// so the box's entry and exit are compared as computed.
 __device__ __forceinline__ bool bvh_box(float3 lo, float3 hi, float3 oa, float3 ob, float3 inv, float limit,
                                         float& entry) {
-    const float lx = (lo.x - oa.x) * inv.x, hx = (hi.x - ob.x) * inv.x;
-    const float ly = (lo.y - oa.y) * inv.y, hy = (hi.y - ob.y) * inv.y;
-    const float lz = (lo.z - oa.z) * inv.z, hz = (hi.z - ob.z) * inv.z;
+    const float lx = __fmaf_rn(lo.x, inv.x, -oa.x), hx = __fmaf_rn(hi.x, inv.x, -ob.x);
+    const float ly = __fmaf_rn(lo.y, inv.y, -oa.y), hy = __fmaf_rn(hi.y, inv.y, -ob.y);
+    const float lz = __fmaf_rn(lo.z, inv.z, -oa.z), hz = __fmaf_rn(hi.z, inv.z, -ob.z);
     const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
     const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
     entry = tmin;
-    return tmax >= -1e-30f - fabsf(tmax) * 3.8146973e-6f && tmin <= tmax + fabsf(tmax) * 3.8146973e-6f &&
-           tmin <= limit;
+    return fmaxf(tmin, 0.0f) <= fminf(tmax, limit);
 }
 
-// One ray's traversal, resumable one node visit at a time (the stack lives
-// with the caller: 64 entries, deeper than any tree Karras' construction
-// builds from 30-bit codes + 32-bit indices).
+// One ray's traversal, resumable one node visit at a time.  The stack lives
+// with the caller: a binary Karras tree over 30-bit codes with 32-bit index
+// tie-breaks is at most 63 deep, the 4-wide tree at most 32, and a visit
+// leaves at most 3 siblings pending per level.
 struct BvhTrav {
-    float3 oa, ob, inv;  // origin grown by +m / -m (see the file comment), 1/d
+    float3 oa, ob, inv;  // (o + m) / d, (o - m) / d per axis (m: see the file comment), 1/d
     float best;          // closest hit so far (+inf: none)
     int bidx;            // its object (-1: none)
     int cur;             // next node to visit; -1 when the traversal is over
     int sp;              // stack depth
 };
 
-constexpr int kBvhStack = 64;
+constexpr int kBvhStack = 96;
 
 __device__ __forceinline__ void bvh_leaf_any(const BvhView& bv, const RayPre& r, bool fast, int obj, float& best,
                                              int& bidx) {
@@ -144,54 +160,96 @@ __device__ __forceinline__ void bvh_begin(const BvhView& bv, const RayPre& r, bo
     const float olen = sqrtf(vdot(r.o, r.o));
     const float far = olen > bv.o_max ? 1.3810679e-3f * 1.001f * (olen - bv.o_max) : 0.0f;  // 2^-9.5
     const float m = far + 9.536743e-7f * (olen + 2.0f * bv.scene_r) + 1e-30f;            // 2^-20
-    T.oa = make_float3(r.o.x + m, r.o.y + m, r.o.z + m);
-    T.ob = make_float3(r.o.x - m, r.o.y - m, r.o.z - m);
-    auto inv1 = [](float v) {
-        const float a = fabsf(v) < 1e-30f ? copysignf(1e-30f, v) : v;
-        return 1.0f / a;
-    };
+    // 1/d clamped to +-cap (a direction component below 1/cap tests its slab
+    // as if it were 1/cap): cap * (|o| + 2R + 1) stays below 1e37, so no
+    // plane distance overflows.
+    const float cap = fminf(1e30f, 1e37f / (olen + 2.0f * bv.scene_r + 1.0f));
+    auto inv1 = [cap](float v) { return fabsf(v) * cap < 1.0f ? copysignf(cap, v) : 1.0f / v; };
     T.inv = make_float3(inv1(r.d.x), inv1(r.d.y), inv1(r.d.z));
+    T.oa = make_float3((r.o.x + m) * T.inv.x, (r.o.y + m) * T.inv.y, (r.o.z + m) * T.inv.z);
+    T.ob = make_float3((r.o.x - m) * T.inv.x, (r.o.y - m) * T.inv.y, (r.o.z - m) * T.inv.z);
     T.cur = 0;
 }
 
-// One node visit of a running traversal (T.cur >= 0): both child boxes,
-// leaf children tested at once, the nearer internal child next and the
-// other pushed; with none, the next stacked box still in front of the best
-// hit, or the end of the traversal (T.cur = -1).
+// Compare-exchange of (entry, node) pairs, ascending by entry.
+__device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb) {
+    const bool sw = kb < ka;
+    const float k = sw ? kb : ka;
+    const int v = sw ? vb : va;
+    kb = sw ? ka : kb;
+    vb = sw ? va : vb;
+    ka = k;
+    va = v;
+}
+
+// One node visit of a running traversal (T.cur >= 0): the four child boxes;
+// leaf children hit are tested at once; the nearest internal child hit is
+// visited next and the others pushed, farthest first; with none, the next
+// stacked box still in front of the best hit, or the end of the traversal
+// (T.cur = -1).
 __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T,
                                          int* stack_node, float* stack_entry, BvhCounters& cnt) {
-    const BvhNode* np = bv.nodes + T.cur;
-    const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c), ndd = __ldg(&np->d);
+    const float4* np = bv.nodes[T.cur].v;
+    float4 lo[4], hi[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        lo[j] = __ldg(np + 2 * j);
+        hi[j] = __ldg(np + 2 * j + 1);
+    }
     ++cnt.visits;
     // limit: skip a box whose entry exceeds best (relative slack for the box test's rounding)
     const float limit = T.best * 1.0000038f + 1e-30f;
-    float e0, e1;
-    bool h0 = bvh_box(make_float3(na.x, na.y, na.z), make_float3(nb.x, nb.y, nb.z), T.oa, T.ob, T.inv, limit, e0);
-    bool h1 = bvh_box(make_float3(nc.x, nc.y, nc.z), make_float3(ndd.x, ndd.y, ndd.z), T.oa, T.ob, T.inv, limit, e1);
-    const int c0 = __float_as_int(na.w), c1 = __float_as_int(nb.w);
-    if (h0 && c0 < 0) {
-        ++cnt.tests;
-        bvh_leaf_any(bv, r, fast, ~c0, T.best, T.bidx);
-        h0 = false;
+    float e[4];
+    int c[4];
+    unsigned hits = 0u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        c[j] = __float_as_int(lo[j].w);
+        if (bvh_box(make_float3(lo[j].x, lo[j].y, lo[j].z), make_float3(hi[j].x, hi[j].y, hi[j].z), T.oa, T.ob,
+                    T.inv, limit, e[j]))
+            hits |= 1u << j;
     }
-    if (h1 && c1 < 0) {
+    unsigned leaves = hits & ((c[0] < 0 ? 1u : 0u) | (c[1] < 0 ? 2u : 0u) | (c[2] < 0 ? 4u : 0u) |
+                              (c[3] < 0 ? 8u : 0u));
+    while (leaves != 0u) {
+        const int j = __ffs(leaves) - 1;
+        leaves &= leaves - 1u;
+        const int cj = j == 0 ? c[0] : j == 1 ? c[1] : j == 2 ? c[2] : c[3];
         ++cnt.tests;
-        bvh_leaf_any(bv, r, fast, ~c1, T.best, T.bidx);
-        h1 = false;
+        bvh_leaf_any(bv, r, fast, ~cj, T.best, T.bidx);
     }
-    if (h0 && h1) {
-        const bool first0 = e0 <= e1;
-        stack_node[T.sp] = first0 ? c1 : c0;
-        stack_entry[T.sp] = first0 ? e1 : e0;
-        ++T.sp;  // depth <= 62 (30 Morton bits + 32 index bits)
-        T.cur = first0 ? c0 : c1;
-    } else if (h0) {
-        T.cur = c0;
-    } else if (h1) {
-        T.cur = c1;
+    // internal children still in front of the (possibly closer) best hit
+    const float lim = T.best * 1.0000038f + 1e-30f;
+    const float INF = __int_as_float(0x7f800000);
+    float k0 = ((hits & 1u) && c[0] >= 0 && e[0] <= lim) ? e[0] : INF;
+    float k1 = ((hits & 2u) && c[1] >= 0 && e[1] <= lim) ? e[1] : INF;
+    float k2 = ((hits & 4u) && c[2] >= 0 && e[2] <= lim) ? e[2] : INF;
+    float k3 = ((hits & 8u) && c[3] >= 0 && e[3] <= lim) ? e[3] : INF;
+    int v0 = c[0], v1 = c[1], v2 = c[2], v3 = c[3];
+    bvh_cswap(k0, v0, k1, v1);
+    bvh_cswap(k2, v2, k3, v3);
+    bvh_cswap(k0, v0, k2, v2);
+    bvh_cswap(k1, v1, k3, v3);
+    bvh_cswap(k1, v1, k2, v2);
+    if (k0 != INF) {
+        if (k3 != INF) {
+            stack_node[T.sp] = v3;
+            stack_entry[T.sp] = k3;
+            ++T.sp;
+        }
+        if (k2 != INF) {
+            stack_node[T.sp] = v2;
+            stack_entry[T.sp] = k2;
+            ++T.sp;
+        }
+        if (k1 != INF) {
+            stack_node[T.sp] = v1;
+            stack_entry[T.sp] = k1;
+            ++T.sp;
+        }
+        T.cur = v0;
     } else {
         // pop the next box still in front of the best hit
-        const float lim = T.best * 1.0000038f + 1e-30f;
         int next = -1;
         while (T.sp > 0) {
             --T.sp;

@@ -51,12 +51,12 @@ struct SceneView {
     float solid[3];
 };
 
-struct BvhNode;  // rdc_bvh.cuh
+struct Bvh4Node;  // rdc_bvh.cuh
 
-// Device LBVH of a scene (rdc_bvh.cu): N-1 nodes (root 0) and 2 records per
-// object in scene order.
+// Device LBVH of a scene (rdc_bvh.cu), collapsed to 4-wide nodes (root 0),
+// and 2 records per object in scene order.
 struct BvhView {
-    const BvhNode* nodes;
+    const Bvh4Node* nodes;
     const float4* prims;
     uint32_t nobj;
     float scene_r;  // bound on |centre| + size over the objects
@@ -64,7 +64,8 @@ struct BvhView {
 };
 
 struct BvhDevice {
-    BvhNode* nodes = nullptr;
+    Bvh4Node* nodes = nullptr;
+    uint32_t nnodes = 0;  // 4-wide nodes
     float4* prims = nullptr;
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -76,7 +77,8 @@ struct BvhDevice {
 };
 
 // Build the LBVH of `sc` on stream `s` (synchronises it).  depth_out: the
-// deepest leaf (the traversal stack holds 64 entries).
+// deepest leaf of the binary tree (at most 63; the 4-wide tree is at most
+// 32 deep and its traversal stack holds 3 entries per level).
 cudaError_t build_lbvh(const struct rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s, uint32_t* depth_out);
 
 struct RenderParams {

@@ -202,13 +202,12 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
             }
         }
         if (__ballot_sync(FULL, pix >= 0) == 0u) break;
-        // Traversal steps until min_idle lanes are done (or all of them).
-        for (;;) {
-            const bool run = in_flight && T.cur >= 0;
-            const unsigned act = __ballot_sync(FULL, run);
-            if (act == 0u) break;
-            if (run) bvh_step(P.bvh, r, rfast, T, stack_node, stack_entry, cnt);
-            if (32u - (unsigned)__popc(__ballot_sync(FULL, in_flight && T.cur >= 0)) >= P.min_idle) break;
+        // Traversal steps until min_idle lanes are done (at least one step).
+        unsigned act = __ballot_sync(FULL, in_flight && T.cur >= 0);
+        while (act != 0u) {
+            if (in_flight && T.cur >= 0) bvh_step(P.bvh, r, rfast, T, stack_node, stack_entry, cnt);
+            act = __ballot_sync(FULL, in_flight && T.cur >= 0);
+            if (32u - (unsigned)__popc(act) >= P.min_idle) break;
         }
     }
     add_warp_sum(P.segments, segs);
