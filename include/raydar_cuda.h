@@ -279,6 +279,31 @@ rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config);
  * Leaves the accumulators of the last trial; render again for results. */
 rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* best_ms_out);
 
+/* ---- differentiation (path-replay adjoint) ------------------------------
+ * The reference renderer is not differentiable; these two calls add the
+ * gradient of an image loss with respect to per-object material parameters,
+ * for the same estimator rdc_render evaluates (src/renderer/cpu.rs:253-341).
+ * The image is the mean radiance, RGB per pixel, row-major (W*H*3 floats). */
+#define RDC_MAX_ADJOINT_BOUNCES 16u
+
+/* Render samples [spp_begin, spp_begin+spp_count) of every pixel from a
+ * cleared accumulator (rdc_reset + rdc_render) and write the mean-radiance
+ * image to image_out (W*H*3 floats; NULL to skip).  Remembers the sample
+ * range, bounce limit and seed for rdc_backward. */
+rdc_status rdc_forward(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces,
+                       uint64_t seed, float* image_out);
+
+/* Gradient of L with respect to every object's parameters, given dl_dimage =
+ * dL/dimage (W*H*3 floats) for the image of the last rdc_forward.  Outputs
+ * (NULL to skip): grad_albedo (N*3), grad_roughness (N, w.r.t.
+ * Material::roughness), grad_emission (N*3, w.r.t. the emitted radiance
+ * emission_color * emission_strength).  Each path is replayed from its
+ * random-number counter; nothing from the forward pass is stored.  Discrete
+ * events (which object a ray hits, which lobe a scatter takes) are held
+ * fixed: roughness moves the gradient only through scatter directions. */
+rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo, float* grad_roughness,
+                        float* grad_emission);
+
 /* Set / get the launch shape of rdc_render.  block_size and blocks_per_sm as
  * for a batch (default 256, 0).  refill_min_idle applies to LBVH renders: a
  * warp keeps stepping its lanes' traversals until this many have finished,

@@ -45,6 +45,10 @@ def load() -> C.CDLL:
     lib.oracle_bounce_words.restype = None
     lib.oracle_uniforms.argtypes = [U32P, C.c_uint32, FP, FP]
     lib.oracle_uniforms.restype = None
+    DP = C.POINTER(C.c_double)
+    lib.oracle_gradient.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, FP,
+                                    DP, DP, DP,
+                                    DP, C.c_int, C.POINTER(C.c_uint64)]
     _lib = lib
     return lib
 
@@ -71,6 +75,29 @@ def render(scene_c, s0, n, max_bounces, seed, accum=None, threads=1, stream=0):
     if rc != 0:
         raise RuntimeError(f"oracle_render failed ({rc})")
     return acc, seg.value
+
+
+def gradient(scene_c, s0, n, max_bounces, seed, dl_dimage, threads=1, stream=0):
+    """FP64 reference gradient of sum(dl_dimage * image), image = mean radiance
+    (HxWx3) of samples [s0, s0+n).  Returns (g_albedo Nx3, g_roughness N,
+    g_emission Nx3, image HxWx3), all float64."""
+    lib = load()
+    w, h = scene_c.desc.camera.resolution_x, scene_c.desc.camera.resolution_y
+    nobj = scene_c.desc.object_count
+    dl = np.ascontiguousarray(dl_dimage, np.float32).reshape(h, w, 3)
+    ga = np.zeros((nobj, 3), np.float64)
+    gr = np.zeros(nobj, np.float64)
+    ge = np.zeros((nobj, 3), np.float64)
+    img = np.zeros((h, w, 3), np.float64)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    lost = C.c_uint64(0)
+    rc = lib.oracle_gradient(_desc(scene_c), s0, n, max_bounces, seed, stream, _f(dl), dp(ga), dp(gr),
+                             dp(ge),
+                             dp(img), threads, C.byref(lost))
+    if rc != 0:
+        raise RuntimeError(f"oracle_gradient failed ({rc})")
+    gradient.lost_paths = lost.value
+    return ga, gr, ge, img
 
 
 def render_pixels(scene_c, pixels, s0, n, max_bounces, seed, accum=None, stream=0):

@@ -53,6 +53,13 @@
 
 namespace oracle {
 
+// Square root, absolute value and sign bit through argument-dependent lookup:
+// the same path code runs on float, double and the forward-mode dual numbers
+// of raydar_oracle_grad.hpp.
+template <typename T> static inline T r_sqrt(T a) { using std::sqrt; return sqrt(a); }
+template <typename T> static inline T r_fabs(T a) { using std::fabs; return fabs(a); }
+template <typename T> static inline bool r_signbit(T a) { using std::signbit; return signbit(a); }
+
 // ---------------------------------------------------------------- vectors --
 template <typename T>
 struct V3 {
@@ -69,7 +76,7 @@ template <typename T> static inline V3<T> neg(V3<T> a) { return {-a.x, -a.y, -a.
 // cgmath InnerSpace::dot: sum of the element-wise product, summed x, y, z in order.
 template <typename T> static inline T dot(V3<T> a, V3<T> b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 template <typename T> static inline T magnitude2(V3<T> a) { return dot(a, a); }
-template <typename T> static inline T magnitude(V3<T> a) { return std::sqrt(magnitude2(a)); }
+template <typename T> static inline T magnitude(V3<T> a) { return r_sqrt(magnitude2(a)); }
 // cgmath normalize = normalize_to(1) = self * (1 / magnitude).
 template <typename T> static inline V3<T> normalize(V3<T> a) { return mul(a, T(1) / magnitude(a)); }
 template <typename T> static inline V3<T> cross(V3<T> a, V3<T> b) {
@@ -82,19 +89,19 @@ template <typename T> static inline V3<T> cross(V3<T> a, V3<T> b) {
 template <typename T> static inline T rmin(T a, T b) {
     if (a != a) return b;
     if (b != b) return a;
-    if (a == b) return std::signbit(a) ? a : b;
+    if (a == b) return r_signbit(a) ? a : b;
     return a < b ? a : b;
 }
 template <typename T> static inline T rmax(T a, T b) {
     if (a != a) return b;
     if (b != b) return a;
-    if (a == b) return std::signbit(a) ? b : a;
+    if (a == b) return r_signbit(a) ? b : a;
     return a > b ? a : b;
 }
 // Rust f32::signum: +-1 by the sign bit (so +-0 map to +-1), NaN stays NaN.
 template <typename T> static inline T rsignum(T a) {
     if (a != a) return a;
-    return std::signbit(a) ? T(-1) : T(1);
+    return r_signbit(a) ? T(-1) : T(1);
 }
 
 // ------------------------------------------------------------- Philox RNG --
@@ -230,7 +237,7 @@ static inline bool hit_sphere(const Ray<T>& ray, V3<T> center, T radius, T* t_ou
     const T c = ((dot(o, o) - T(2) * dot(o, center)) + dot(center, center)) - radius * radius;
     const T disc = k * k - a * c;
     if (disc < T(0)) return false;
-    const T sq = std::sqrt(disc);
+    const T sq = r_sqrt(disc);
     const T t1 = (-k - sq) / a;
     const T t2 = (-k + sq) / a;
     if (t1 >= T(0)) {
@@ -294,9 +301,9 @@ static inline void closest_hit(const Ray<T>& ray, T t, const Object<T>& ob, Hit<
     } else {
         const V3<T> lp = sub(p, ob.center);
         const T hs = ob.side_length / T(2);
-        const T xd = std::fabs(std::fabs(lp.x) - hs);
-        const T yd = std::fabs(std::fabs(lp.y) - hs);
-        const T zd = std::fabs(std::fabs(lp.z) - hs);
+        const T xd = r_fabs(r_fabs(lp.x) - hs);
+        const T yd = r_fabs(r_fabs(lp.y) - hs);
+        const T zd = r_fabs(r_fabs(lp.z) - hs);
         if (xd < yd && xd < zd)
             n = v3(rsignum(lp.x), T(0), T(0));
         else if (yd < zd)
@@ -343,7 +350,7 @@ template <typename T>
 static inline V3<T> refract(V3<T> v, V3<T> n, T ratio) {
     const T cos_theta = rmin(dot(v, neg(n)), T(1));
     const V3<T> perp = mul(add(v, mul(n, cos_theta)), ratio);
-    const T s = -std::sqrt(std::fabs(T(1) - magnitude2(perp)));
+    const T s = -r_sqrt(r_fabs(T(1) - magnitude2(perp)));
     const V3<T> par = mul(n, s);
     return add(perp, par);
 }
@@ -352,7 +359,7 @@ static inline V3<T> refract(V3<T> v, V3<T> n, T ratio) {
 template <typename T>
 static inline bool can_refract(V3<T> v, V3<T> n, T ratio) {
     const T cos_theta = rmin(dot(v, neg(n)), T(1));
-    const T sin_theta = std::sqrt(T(1) - cos_theta * cos_theta);
+    const T sin_theta = r_sqrt(T(1) - cos_theta * cos_theta);
     return ratio * sin_theta <= T(1);
 }
 
@@ -374,25 +381,37 @@ static inline V3<T> world_sample(const Scene<T>& s, V3<T> d) {
     return add(s.bottom, mul(sub(s.top, s.bottom), amt));  // cgmath lerp
 }
 
+// The discrete choices of one scatter: which lobe, the diffuse flip, the
+// transmission branch and the |dir|^2 < 1e-10 fallback.  The gradient oracle
+// records them on the float path and replays that path in double with them
+// held fixed (the same estimator, evaluated at higher precision).
+enum { kLobeDiffuse = 0, kLobeSpecular = 1, kLobeRefract = 2 };
+struct Choice {
+    int lobe;
+    bool flip, trans, to_normal;
+};
+
 // The hit branch of per_pixel, src/renderer/cpu.rs:262-333, given the
-// bounce's random words.  Updates the ray; returns the object's albedo and
-// emission for the caller's attenuation / light update.
+// bounce's random words.  Updates the ray.  ch: if force, the choices to
+// take; else, when not null, receives the choices taken.
 template <typename T>
 static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& ob,
-                           const uint32_t* w, Ray<T>* out) {
+                           const uint32_t* w, Ray<T>* out, Choice* ch = nullptr, bool force = false) {
     const T roughness = ob.roughness * ob.roughness;
     const T metallic = ob.metallic;
     const T transmission = ob.transmission;
 
     V3<T> diffuse = add(h.normal, random_in_unit_sphere<T>(w + 0));
-    if (dot(diffuse, h.normal) < T(0)) diffuse = neg(diffuse);
+    const bool flip = force ? ch->flip : dot(diffuse, h.normal) < T(0);
+    if (flip) diffuse = neg(diffuse);
 
     const V3<T> perfect = reflect(ray.direction, h.normal);
     const V3<T> offset2 = mul(random_in_unit_sphere<T>(w + 3), roughness);
     const V3<T> specular = normalize(add(perfect, offset2));
 
-    const bool transmission_ray = (T)uniform01(w[6]) < transmission;
+    const bool transmission_ray = force ? ch->trans : (T)uniform01(w[6]) < transmission;
     V3<T> direction;
+    int lobe = kLobeSpecular;
     if (transmission_ray) {
         T ior = ob.ior;
         if (h.front) ior = T(1) / ior;
@@ -404,25 +423,33 @@ static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& 
         const T m2 = m * m;
         const T m5 = m * (m2 * m2);                  // powi(5), square-and-multiply
         const T refl = r0 + (T(1) - r0) * m5;
-        if (refl < (T)uniform01(w[7]) && can_refract(rd, h.normal, ior)) {
+        const bool refr = force ? ch->lobe == kLobeRefract
+                                : (refl < (T)uniform01(w[7]) && can_refract(rd, h.normal, ior));
+        if (refr) {
             const V3<T> refracted = refract(rd, h.normal, ior);
             const V3<T> offset3 = mul(random_in_unit_sphere<T>(w + 8), roughness);
             direction = normalize(add(refracted, offset3));
+            lobe = kLobeRefract;
         } else {
             direction = specular;
         }
-    } else if ((T)uniform01(w[7]) < metallic) {
+    } else if (force ? ch->lobe == kLobeSpecular && (T)uniform01(w[7]) < metallic
+                     : (T)uniform01(w[7]) < metallic) {
         direction = specular;
     } else {
-        if ((T)uniform01(w[8]) < roughness)
+        if (force ? ch->lobe == kLobeDiffuse : (T)uniform01(w[8]) < roughness) {
             direction = diffuse;
-        else
+            lobe = kLobeDiffuse;
+        } else {
             direction = specular;
+        }
     }
     const V3<T> off = transmission_ray ? direction : h.normal;
     out->origin = add(h.position, mul(off, T(0.0001f)));
     out->direction = direction;
-    if (magnitude2(out->direction) < T(1e-10f)) out->direction = h.normal;
+    const bool to_normal = force ? ch->to_normal : magnitude2(out->direction) < T(1e-10f);
+    if (to_normal) out->direction = h.normal;
+    if (ch && !force) *ch = Choice{lobe, flip, transmission_ray, to_normal};
 }
 
 // Primary ray of pixel (x, y): src/renderer/cpu.rs:199-202, 234-251.

@@ -1,0 +1,234 @@
+// raydar_oracle_grad.hpp -- FP64 reference gradient of an image loss (TEST
+// INFRASTRUCTURE ONLY: the checker of the CUDA adjoint).
+//
+// The estimator is the forward path of raydar_oracle.hpp (src/renderer/cpu.rs:
+// 253-341) evaluated in double, with the same Philox words per bounce.  A
+// path's radiance is
+//     L = sum_k E(obj_k) + [miss after K hits] sky(d_K) * prod_k albedo(obj_k)
+// (emission is added without attenuation, cpu.rs:330-341).  Its derivatives:
+//   - emission E (the emitted radiance emission_color * emission_strength):
+//     dL/dE(j) = number of hits on j;
+//   - albedo: dL_c/dalbedo_c(j) = sky_c * sum over hits k on j of the product
+//     of the other hits' albedos;
+//   - roughness: only through the miss direction d_K, which every scatter
+//     after the first roughness use moves.  Computed here by forward-mode
+//     automatic differentiation: the roughness of the object hit at bounce k
+//     is seeded as tangent slot k of a dual number, and the unchanged path
+//     code (intersection, normal, reflect, refract, normalize, sky) carries
+//     the tangents.  This is a different derivation from the CUDA backward
+//     kernel's hand-written reverse sweep, so the two check each other.
+// Discrete choices (which object is hit, which lobe, the diffuse flip, the
+// front face) are those of the float path, recorded first and then held
+// fixed: the gradient of the same path-replay estimator the CUDA kernels
+// evaluate, computed in double.  (Re-deciding them in double would follow a
+// different path wherever float and double rounding part ways, which after a
+// few bounces off curved mirrors is common.)
+#pragma once
+
+#include <cmath>
+
+#include "raydar_oracle.hpp"
+
+namespace oracle {
+
+constexpr int kGradSlots = 16;  // bounces with a roughness tangent slot each
+
+// Forward-mode dual number: a value and kGradSlots partial derivatives.
+struct Dual {
+    double v;
+    double d[kGradSlots];
+    Dual() : v(0.0) {
+        for (int i = 0; i < kGradSlots; ++i) d[i] = 0.0;
+    }
+    Dual(double x) : v(x) {  // NOLINT: implicit, as the path code writes T(2), T(0.0001f)
+        for (int i = 0; i < kGradSlots; ++i) d[i] = 0.0;
+    }
+};
+
+inline Dual operator+(const Dual& a, const Dual& b) {
+    Dual r(a.v + b.v);
+    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+inline Dual operator-(const Dual& a, const Dual& b) {
+    Dual r(a.v - b.v);
+    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+inline Dual operator-(const Dual& a) {
+    Dual r(-a.v);
+    for (int i = 0; i < kGradSlots; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+inline Dual operator*(const Dual& a, const Dual& b) {
+    Dual r(a.v * b.v);
+    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+inline Dual operator/(const Dual& a, const Dual& b) {
+    Dual r(a.v / b.v);
+    const double inv = 1.0 / b.v;
+    for (int i = 0; i < kGradSlots; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * inv;
+    return r;
+}
+inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+inline bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
+inline bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
+
+// Found by argument-dependent lookup from r_sqrt / r_fabs / r_signbit.
+inline Dual sqrt(const Dual& a) {
+    Dual r(std::sqrt(a.v));
+    const double g = r.v > 0.0 ? 0.5 / r.v : 0.0;
+    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] * g;
+    return r;
+}
+inline Dual fabs(const Dual& a) { return std::signbit(a.v) ? -a : a; }
+inline bool signbit(const Dual& a) { return std::signbit(a.v); }
+
+// One path's discrete history on the float path: the object hit, its front
+// flag and the scatter choices per bounce, and whether it ended in a miss.
+struct PathRecord {
+    int nv = 0;
+    bool missed = false;
+    int obj[kGradSlots];
+    bool front[kGradSlots];
+    Choice ch[kGradSlots];
+    V3<float> o[kGradSlots], d[kGradSlots];  // the ray reaching each vertex
+    float t[kGradSlots];
+    V3<float> d_end;  // the direction after the last vertex
+};
+
+// The float path of trace_path (src/renderer/cpu.rs:253-341), recorded.
+inline void record_path(const Scene<float>& s, Ray<float> ray, uint32_t max_bounces, uint64_t seed,
+                        uint32_t stream, uint32_t pixel, uint32_t sample, PathRecord* rec) {
+    rec->nv = 0;
+    rec->missed = false;
+    for (uint32_t b = 0; b < max_bounces; ++b) {
+        rec->d_end = ray.direction;
+        const Hit<float> h = trace_ray(ray, s);
+        if (h.index < 0) {
+            rec->missed = true;
+            return;
+        }
+        rec->o[rec->nv] = ray.origin;
+        rec->d[rec->nv] = ray.direction;
+        rec->t[rec->nv] = h.t;
+        uint32_t w[12];
+        bounce_words(seed, stream, pixel, sample, b, w);
+        Ray<float> next;
+        scatter(ray, h, s.objects[h.index], w, &next, &rec->ch[rec->nv]);
+        rec->obj[rec->nv] = h.index;
+        rec->front[rec->nv] = h.front;
+        ++rec->nv;
+        ray = next;
+    }
+    rec->d_end = ray.direction;
+}
+
+// A dual number with its value replaced and its tangents kept.
+inline Dual at_value(const Dual& a, double v) {
+    Dual r = a;
+    r.v = v;
+    return r;
+}
+inline V3<Dual> at_value(const V3<Dual>& a, V3<float> v) {
+    return v3(at_value(a.x, v.x), at_value(a.y, v.y), at_value(a.z, v.z));
+}
+
+// Gradient of sum_p,c dL_dimage[p,c] * image[p,c] with image = the mean
+// radiance of samples [s0, s0+n) of pixel p, for the pixels in [p0, p1).
+// Each path is traced in float to fix its discrete history and its points;
+// the tangents are then carried in double along that history, each vertex
+// evaluated at the float path's ray and hit distance (re-tracing the values
+// in double would drift from the float path by rounding that a few bounces
+// off curved surfaces amplify, and the derivative would be taken elsewhere).  Adds into
+// g_albedo (N*3), g_rough (N), g_emission (N*3); writes the mean image (RGB,
+// double) of those pixels into image (npix*3) when it is not null.  Returns
+// the number of paths whose double evaluation lost a recorded hit (grazing
+// rays; they add no albedo or roughness term).
+inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, uint32_t p0, uint32_t p1,
+                                uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed, uint32_t stream,
+                                const float* dl_dimage, double* g_albedo, double* g_rough, double* g_emission,
+                                double* image) {
+    uint64_t lost = 0;
+    for (uint32_t pix = p0; pix < p1; ++pix) {
+        const Ray<float> prim_f = primary_ray(sf, pix % s.width, pix / s.width);
+        const Ray<Dual> prim = primary_ray(s, pix % s.width, pix / s.width);
+        double w[3], img[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < 3; ++c) w[c] = (double)dl_dimage[3 * (size_t)pix + c] / (double)n;
+        for (uint32_t k = 0; k < n; ++k) {
+            PathRecord rec;
+            record_path(sf, prim_f, max_bounces, seed, stream, pix, s0 + k, &rec);
+            Ray<Dual> ray = prim;
+            bool ok = true;
+            for (int v = 0; v < rec.nv && ok; ++v) {
+                Object<Dual> ob = s.objects[rec.obj[v]];
+                // evaluate at the float path's ray and hit distance, with the
+                // tangents carried in double
+                ray.origin = at_value(ray.origin, rec.o[v]);
+                ray.direction = at_value(ray.direction, rec.d[v]);
+                Dual t;
+                if (!hit_object(ray, ob, &t)) {
+                    ok = false;
+                    break;
+                }
+                t = at_value(t, rec.t[v]);
+                Hit<Dual> h;
+                h.index = rec.obj[v];
+                closest_hit(ray, t, ob, &h);
+                if (h.front != rec.front[v]) {  // grazing: keep the float path's side
+                    h.front = rec.front[v];
+                    h.normal = neg(h.normal);
+                }
+                ob.roughness.d[v] = 1.0;  // tangent slot v: this bounce's roughness
+                uint32_t words[12];
+                bounce_words(seed, stream, pix, s0 + k, (uint32_t)v, words);
+                Ray<Dual> next;
+                scatter(ray, h, ob, words, &next, &rec.ch[v], true);
+                ray = next;
+            }
+            double light[3] = {0.0, 0.0, 0.0};
+            for (int v = 0; v < rec.nv; ++v) {
+                const Object<Dual>& ob = s.objects[rec.obj[v]];
+                const double e[3] = {ob.emission_color.x.v * ob.emission_strength.v,
+                                     ob.emission_color.y.v * ob.emission_strength.v,
+                                     ob.emission_color.z.v * ob.emission_strength.v};
+                for (int c = 0; c < 3; ++c) {
+                    light[c] += e[c];
+                    g_emission[3 * (size_t)rec.obj[v] + c] += w[c];
+                }
+            }
+            if (!ok) ++lost;
+            if (rec.missed && ok) {
+                const V3<Dual> sky = world_sample(s, at_value(ray.direction, rec.d_end));
+                const Dual skyc[3] = {sky.x, sky.y, sky.z};
+                for (int c = 0; c < 3; ++c) {
+                    double alb[kGradSlots];
+                    double prod = 1.0;
+                    for (int v = 0; v < rec.nv; ++v) {
+                        const V3<Dual>& a = s.objects[rec.obj[v]].albedo;
+                        alb[v] = c == 0 ? a.x.v : (c == 1 ? a.y.v : a.z.v);
+                        prod *= alb[v];
+                    }
+                    light[c] += skyc[c].v * prod;
+                    for (int v = 0; v < rec.nv; ++v) {
+                        double others = 1.0;
+                        for (int m = 0; m < rec.nv; ++m)
+                            if (m != v) others *= alb[m];
+                        g_albedo[3 * (size_t)rec.obj[v] + c] += w[c] * skyc[c].v * others;
+                        g_rough[rec.obj[v]] += w[c] * prod * skyc[c].d[v];
+                    }
+                }
+            }
+            for (int c = 0; c < 3; ++c) img[c] += light[c];
+        }
+        if (image)
+            for (int c = 0; c < 3; ++c) image[3 * (size_t)pix + c] = img[c] / (double)n;
+    }
+    return lost;
+}
+
+}  // namespace oracle

@@ -1,0 +1,346 @@
+// rdc_adjoint.cu -- path-replay adjoint of the render (sm_103a).
+//
+// The loss is any function of the mean-radiance image; the caller passes
+// dL/dimage (RGB per pixel).  A path of pixel p contributes
+//     L = sum_k E(obj_k) + [miss after K hits] sky(d_K) * prod_k albedo(obj_k)
+// (src/renderer/cpu.rs:253-341: emission is added without attenuation, the
+// miss adds the sky times the albedo product), weighted by
+// dL/dimage(p) / spp.  Gradients per object:
+//   - emission E = emission_color * emission_strength: the weight, once per hit;
+//   - albedo: weight * sky * the product of the path's other albedos;
+//   - roughness^2 (the host applies d(r^2)/dr = 2r): only through the miss
+//     direction d_K.  The kernel seeds the adjoint of d_K with the sky's
+//     derivative and sweeps the path's vertices in reverse, through the
+//     scatter (normalize, reflect, refract), the front-face flip, the sphere
+//     normal and the ray parameter t (implicit differentiation of the hit
+//     surface), accumulating each vertex's roughness term.
+// Discrete choices (the object hit, the lobe, the diffuse flip) are not
+// differentiated: this is the gradient of the path-replay estimator.
+//
+// Nothing of the forward pass is stored: each path is replayed from its
+// Philox counter (pixel, sample, bounce) with the forward kernels' own
+// functions, so it retraces the rendered path bit for bit, into a per-thread
+// record of at most kAdjMaxBounces vertices.  Gradients are summed per warp
+// over lanes that hit the same object (match + pointer-jumping reduction)
+// and added with FP32 atomics, into per-block shared accumulators when the
+// scene's gradient table fits, else straight into global memory.
+#include <cstdint>
+
+#include "rdc_bvh.cuh"
+#include "rdc_device.cuh"
+
+namespace rdc {
+
+namespace {
+
+struct AdjVert {
+    V3 o, d;       // incoming ray
+    float t;       // hit distance; after the sweep: dL/d(roughness^2) of this vertex
+    int obj;
+    uint32_t flags;  // ScatterRec flags
+    V3 s;          // unit-sphere vector of the lobe
+    V3 pre;        // product of the albedos before this vertex; after the sweep: dL/dalbedo
+};
+
+// Reverse step through vertex v: (go, gd) are the adjoints of the ray that
+// leaves v; returns those of the ray that reaches v and dL/d(roughness^2).
+__device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& v, V3& go, V3& gd) {
+    const MatDev m = sc.mat[v.obj];
+    const float4 hi = __ldg(&sc.hit[v.obj]);
+    const int kind = __float_as_int(m.d.y);
+    const HitRec h = closest_hit(v.o, v.d, v.t, hi, kind);
+    const float r = m.a.w;
+    const uint32_t f = v.flags;
+    const V3 d = v.d, n = h.n;
+    V3 g_dir = mk(0.f, 0.f, 0.f), g_n = mk(0.f, 0.f, 0.f);
+    if (f & kScatNormal)
+        g_n = gd;
+    else
+        g_dir = gd;
+    if (f & kScatTrans)
+        g_dir = vadd(g_dir, vmul(go, 0.0001f));
+    else
+        g_n = vadd(g_n, vmul(go, 0.0001f));
+    V3 g_p = go, g_din = mk(0.f, 0.f, 0.f);
+    float gr = 0.0f;
+    const uint32_t lobe = f & 3u;
+    if (lobe == kLobeDiffuse) {
+        g_n = (f & kScatFlip) ? vsub(g_n, g_dir) : vadd(g_n, g_dir);  // dir = +-(n + s1)
+    } else if (lobe == kLobeSpecular) {
+        // dir = X / |X|, X = d - 2 (d.n) n + s2 r
+        const float dn = vdot(d, n);
+        const V3 X = vadd(vsub(d, vmul(n, 2.0f * dn)), vmul(v.s, r));
+        const float L = sqrtf(vdot(X, X));
+        const V3 u = vmul(X, 1.0f / L);
+        const V3 gX = vmul(vsub(g_dir, vmul(u, vdot(g_dir, u))), 1.0f / L);
+        gr += vdot(v.s, gX);
+        const float ngX = vdot(n, gX);
+        g_din = vadd(g_din, vsub(gX, vmul(n, 2.0f * ngX)));
+        g_n = vsub(g_n, vadd(vmul(gX, 2.0f * dn), vmul(d, 2.0f * ngX)));
+    } else {
+        // dir = Z / |Z|, Z = perp + s n + s3 r, perp = ratio (rd + cos n),
+        // s = -sqrt|1 - perp.perp|, cos = min(-rd.n, 1), rd = d / |d|
+        const float ratio = (f & kScatFront) ? m.c.y : m.c.z;
+        const float dl = sqrtf(vdot(d, d));
+        const V3 rd = vmul(d, 1.0f / dl);
+        const float cr = -vdot(rd, n);
+        const float cs = fminf(cr, 1.0f);
+        const V3 perp = vmul(vadd(rd, vmul(n, cs)), ratio);
+        const float q = 1.0f - vdot(perp, perp);
+        const float sq = sqrtf(fabsf(q));
+        const V3 Z = vadd(vadd(perp, vmul(n, -sq)), vmul(v.s, r));
+        const float L = sqrtf(vdot(Z, Z));
+        const V3 u = vmul(Z, 1.0f / L);
+        const V3 gZ = vmul(vsub(g_dir, vmul(u, vdot(g_dir, u))), 1.0f / L);
+        gr += vdot(v.s, gZ);
+        V3 g_perp = gZ;
+        const float gs = vdot(n, gZ);
+        g_n = vadd(g_n, vmul(gZ, -sq));
+        if (sq > 1e-12f) g_perp = vadd(g_perp, vmul(perp, gs * (q < 0.0f ? -1.0f : 1.0f) / sq));
+        V3 g_rd = vmul(g_perp, ratio);
+        const float gcos = ratio * vdot(n, g_perp);
+        g_n = vadd(g_n, vmul(g_perp, ratio * cs));
+        if (cr < 1.0f) {
+            g_rd = vsub(g_rd, vmul(n, gcos));
+            g_n = vsub(g_n, vmul(rd, gcos));
+        }
+        g_din = vadd(g_din, vmul(vsub(g_rd, vmul(rd, vdot(g_rd, rd))), 1.0f / dl));
+    }
+    // n = +-n0 (front-face flip); sphere n0 = (p - c) / |p - c|, cube n0 constant
+    const V3 g_n0 = h.front ? g_n : vneg(g_n);
+    const V3 c = mk(hi.x, hi.y, hi.z);
+    const V3 pc = vsub(h.p, c);
+    if (kind == 0) {
+        const float pl = sqrtf(vdot(pc, pc));
+        const V3 n0 = vmul(pc, 1.0f / pl);
+        g_p = vadd(g_p, vmul(vsub(g_n0, vmul(n0, vdot(g_n0, n0))), 1.0f / pl));
+    }
+    // p = o + t d with t(o, d) on the hit surface
+    const float g_t = vdot(g_p, d);
+    V3 go_new = g_p;
+    V3 gd_new = vadd(g_din, vmul(g_p, v.t));
+    if (kind == 0) {
+        // |o + t d - c|^2 = r^2:  dt = -(p - c).(do + t dd) / ((p - c).d)
+        const float den = vdot(pc, d);
+        if (fabsf(den) > 1e-20f) {
+            const float k = g_t / den;
+            go_new = vsub(go_new, vmul(pc, k));
+            gd_new = vsub(gd_new, vmul(pc, k * v.t));
+        }
+    } else {
+        // the hit face's plane x_i = const:  dt = -(do_i + t dd_i) / d_i
+        const int ax = n.x != 0.0f ? 0 : (n.y != 0.0f ? 1 : 2);
+        const float di = ax == 0 ? d.x : (ax == 1 ? d.y : d.z);
+        if (fabsf(di) > 1e-20f) {
+            const float k = g_t / di;
+            if (ax == 0) {
+                go_new.x -= k;
+                gd_new.x -= k * v.t;
+            } else if (ax == 1) {
+                go_new.y -= k;
+                gd_new.y -= k * v.t;
+            } else {
+                go_new.z -= k;
+                gd_new.z -= k * v.t;
+            }
+        }
+    }
+    go = go_new;
+    gd = gd_new;
+    return gr;
+}
+
+// Sum c[0..6] over the lanes of the warp with the same obj (>= 0) and add
+// the sums at g + 8 * obj with one atomic per object and component: the
+// lanes sharing an object form a list in lane order, and pointer jumping
+// (5 rounds) leaves the list's total with its first lane.
+__device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7]) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(FULL, obj);
+    const unsigned above = lane == 31 ? 0u : (peers & (0xffffffffu << (lane + 1)));
+    int next = above ? __ffs(above) - 1 : lane;
+    bool has = above != 0u;
+#pragma unroll
+    for (int round = 0; round < 5; ++round) {
+        float o[7];
+#pragma unroll
+        for (int j = 0; j < 7; ++j) o[j] = __shfl_sync(FULL, c[j], next);
+        const int nn = __shfl_sync(FULL, next, next);
+        const bool nh = __shfl_sync(FULL, has ? 1 : 0, next) != 0;
+        if (has) {
+#pragma unroll
+            for (int j = 0; j < 7; ++j) c[j] += o[j];
+            next = nn;
+            has = nh;
+        }
+    }
+    if (obj >= 0 && lane == __ffs(peers) - 1) {
+        float* dst = g + 8 * (size_t)obj;
+#pragma unroll
+        for (int j = 0; j < 7; ++j)
+            if (c[j] != 0.0f) atomicAdd(dst + j, c[j]);
+    }
+}
+
+template <bool kBvh>
+__global__ void __launch_bounds__(kRenderBlock, 2) adjoint_kernel(const AdjParams P) {
+    extern __shared__ float4 smem[];
+    const unsigned FULL = 0xffffffffu;
+    float4* s_rec = smem;
+    int4* s_runs = reinterpret_cast<int4*>(smem + (kBvh ? 0u : P.sc.nrec));
+    float* s_grad = reinterpret_cast<float*>(s_runs + (kBvh ? 0u : P.sc.nruns));
+    if (!kBvh) {
+        for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
+        for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
+    }
+    if (P.smem_grad)
+        for (uint32_t i = threadIdx.x; i < 8u * P.sc.nobj; i += blockDim.x) s_grad[i] = 0.0f;
+    __syncthreads();
+    float* gbase = P.smem_grad ? s_grad : P.grad;
+    const bool scene_fast = P.sc.fast_div != 0u;
+    BruteIsect brute{s_rec, s_runs, (int)P.sc.nruns, scene_fast};
+    BvhCounters cnt;
+    uint32_t segs = 0;
+
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t rounds = (P.npaths + stride - 1) / stride;  // the same for every thread
+    for (uint64_t it = 0; it < rounds; ++it) {
+        const uint64_t path = it * stride + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        AdjVert v[kAdjMaxBounces];
+        int nv = 0;
+        V3 gw = mk(0.f, 0.f, 0.f);
+        if (path < P.npaths) {
+            const uint32_t pix = (uint32_t)(path / P.nspp);
+            const uint32_t sample = P.s0 + (uint32_t)(path % P.nspp);
+            const float inv_n = 1.0f / (float)P.nspp;
+            gw = mk(P.dl[3 * (size_t)pix] * inv_n, P.dl[3 * (size_t)pix + 1] * inv_n,
+                    P.dl[3 * (size_t)pix + 2] * inv_n);
+            if (gw.x != 0.0f || gw.y != 0.0f || gw.z != 0.0f) {
+                // replay (the forward kernels' arithmetic, bit for bit)
+                V3 o, d;
+                primary_ray(P.sc, pix % P.sc.width, pix / P.sc.width, o, d);
+                V3 atten = mk(1.f, 1.f, 1.f);
+                bool missed = false;
+                for (uint32_t b = 0; b < P.max_bounces; ++b) {
+                    ++segs;
+                    const RayPre r = ray_pre(o, d, P.sc.neg_zero);
+                    float t;
+                    int idx;
+                    if (kBvh)
+                        bvh_intersect(P.bvh, r, scene_fast && r.fast, t, idx, cnt);
+                    else
+                        brute(r, t, idx);
+                    if (idx < 0) {
+                        missed = true;
+                        break;
+                    }
+                    const MatDev m = P.sc.mat[idx];
+                    const HitRec h = closest_hit(o, d, t, __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
+                    uint32_t w[12];
+                    const uint32_t c2 = b * 4u;
+                    const U4 w0 = philox(pix, sample, c2, P.stream_id, P.key0, P.key1);
+                    const U4 w1 = philox(pix, sample, c2 + 1u, P.stream_id, P.key0, P.key1);
+                    const U4 w2 = philox(pix, sample, c2 + 2u, P.stream_id, P.key0, P.key1);
+                    w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
+                    w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
+                    w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
+                    ScatterRec rec;
+                    V3 no, nd;
+                    scatter_impl<true>(d, h, m, w, no, nd, &rec);
+                    AdjVert& vk = v[nv++];
+                    vk.o = o;
+                    vk.d = d;
+                    vk.t = t;
+                    vk.obj = idx;
+                    vk.flags = rec.flags;
+                    vk.s = rec.s;
+                    vk.pre = atten;
+                    atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
+                    o = no;
+                    d = nd;
+                }
+                // reverse sweep
+                if (missed) {
+                    const V3 sky = world_sample(P.sc, d);
+                    V3 go = mk(0.f, 0.f, 0.f), gd = mk(0.f, 0.f, 0.f);
+                    if (P.sc.world_kind == 0u) {
+                        // sky = bottom + (top - bottom) (d.y / |d| + 1) / 2
+                        const float coef = 0.5f * (gw.x * atten.x * (P.sc.top[0] - P.sc.bottom[0]) +
+                                                   gw.y * atten.y * (P.sc.top[1] - P.sc.bottom[1]) +
+                                                   gw.z * atten.z * (P.sc.top[2] - P.sc.bottom[2]));
+                        const float len = sqrtf(vdot(d, d));
+                        const float cosv = d.y / len;
+                        gd = vmul(vsub(mk(0.f, 1.f, 0.f), vmul(d, cosv / len)), coef / len);
+                    }
+                    V3 suf = mk(1.f, 1.f, 1.f);
+                    for (int k = nv - 1; k >= 0; --k) {
+                        AdjVert& vk = v[k];
+                        const float4 alb = P.sc.mat[vk.obj].a;
+                        const V3 ga = mk(gw.x * sky.x * vk.pre.x * suf.x, gw.y * sky.y * vk.pre.y * suf.y,
+                                         gw.z * sky.z * vk.pre.z * suf.z);
+                        suf = mk(suf.x * alb.x, suf.y * alb.y, suf.z * alb.z);
+                        vk.t = vertex_vjp(P.sc, vk, go, gd);
+                        vk.pre = ga;
+                    }
+                } else {
+                    for (int k = 0; k < nv; ++k) {
+                        v[k].t = 0.0f;
+                        v[k].pre = mk(0.f, 0.f, 0.f);
+                    }
+                }
+            }
+        }
+        // warp-converged accumulation over vertex slots
+        const int maxnv = (int)__reduce_max_sync(FULL, (unsigned)nv);
+        for (int k = 0; k < maxnv; ++k) {
+            const bool has = k < nv;
+            const int obj = has ? v[k].obj : -1;
+            float c[7];
+            c[0] = has ? v[k].pre.x : 0.0f;
+            c[1] = has ? v[k].pre.y : 0.0f;
+            c[2] = has ? v[k].pre.z : 0.0f;
+            c[3] = has ? gw.x : 0.0f;
+            c[4] = has ? gw.y : 0.0f;
+            c[5] = has ? gw.z : 0.0f;
+            c[6] = has ? v[k].t : 0.0f;
+            warp_add_grad(gbase, obj, c);
+        }
+    }
+    // flush the block's shared accumulators; counters
+    if (P.smem_grad) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < 8u * P.sc.nobj; i += blockDim.x)
+            if (s_grad[i] != 0.0f) atomicAdd(P.grad + i, s_grad[i]);
+    }
+    unsigned long long s = segs;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
+    if ((threadIdx.x & 31) == 0 && s != 0ull) atomicAdd(P.segments, s);
+}
+
+}  // namespace
+
+size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad) {
+    size_t b = bvh ? 0 : 16u * ((size_t)sc.nrec + sc.nruns);
+    if (smem_grad) b += 32u * (size_t)sc.nobj;
+    return b;
+}
+
+cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm) {
+    const void* fn = bvh ? (const void*)adjoint_kernel<true> : (const void*)adjoint_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+}
+
+cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, size_t smem, cudaStream_t s) {
+    if (bvh)
+        adjoint_kernel<true><<<grid, block, smem, s>>>(p);
+    else
+        adjoint_kernel<false><<<grid, block, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace rdc

@@ -63,6 +63,14 @@ struct rdc_ctx {
     std::vector<rdc_object> host_objects;  // copy of the uploaded scene (LBVH rebuilds)
     rdc_scene_desc host_desc{};
 
+    // differentiation (rdc_forward / rdc_backward)
+    bool adj_valid = false;
+    uint32_t adj_s0 = 0, adj_n = 0, adj_bounces = 0;
+    uint64_t adj_seed = 0;
+    float* d_grad = nullptr;
+    float* d_dl = nullptr;
+    size_t cap_grad = 0, cap_dl = 0;
+
     // batch (rdc_batch_upload)
     struct Batch {
         uint32_t n = 0;
@@ -278,6 +286,8 @@ void rdc_destroy(rdc_ctx* ctx) {
     cudaFree(ctx->d_accum);
     cudaFree(ctx->d_rgba);
     cudaFree(ctx->d_counters);
+    cudaFree(ctx->d_grad);
+    cudaFree(ctx->d_dl);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -362,6 +372,7 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
         ctx->sample_count = 0;
     }
     ctx->has_scene = true;
+    ctx->adj_valid = false;
     return RDC_OK;
 }
 
@@ -512,6 +523,103 @@ rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out) {
     out->kernel_launches = ctx->last_launches;
     out->h2d_bytes = ctx->h2d_bytes;
     out->d2h_bytes = ctx->d2h_bytes;
+    return RDC_OK;
+}
+
+rdc_status rdc_forward(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces, uint64_t seed,
+                       float* image_out) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_forward: no scene uploaded");
+    if (spp_count == 0) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_forward: spp_count is 0");
+    if (max_bounces > rdc::kAdjMaxBounces)
+        return fail(ctx, RDC_ERR_LIMIT, "rdc_forward: max_bounces above RDC_MAX_ADJOINT_BOUNCES");
+    if (rdc_status st = rdc_reset(ctx)) return st;
+    if (rdc_status st = rdc_render(ctx, spp_begin, spp_count, max_bounces, seed)) return st;
+    ctx->adj_valid = true;
+    ctx->adj_s0 = spp_begin;
+    ctx->adj_n = spp_count;
+    ctx->adj_bounces = max_bounces;
+    ctx->adj_seed = seed;
+    if (!image_out) return RDC_OK;
+    const size_t npix = (size_t)ctx->width * ctx->height;
+    std::vector<float> acc(npix * 4);
+    if (rdc_status st = rdc_read_accum(ctx, acc.data(), acc.size())) return st;
+    const float inv = 1.0f / (float)spp_count;
+    for (size_t i = 0; i < npix; ++i)
+        for (int c = 0; c < 3; ++c) image_out[3 * i + c] = acc[4 * i + c] * inv;
+    return RDC_OK;
+}
+
+rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo, float* grad_roughness,
+                        float* grad_emission) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_backward: no scene uploaded");
+    if (!ctx->adj_valid)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_backward: no rdc_forward since the scene was uploaded");
+    if (!dl_dimage) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_backward: dl_dimage is NULL");
+    if (rdc_status st = set_device(ctx)) return st;
+    const uint32_t nobj = ctx->host_desc.object_count;
+    const size_t npix = (size_t)ctx->width * ctx->height;
+    if (rdc_status st = ensure(ctx, &ctx->d_dl, &ctx->cap_dl, npix * 3, "rdc_backward: dL/dimage")) return st;
+    if (rdc_status st = ensure(ctx, &ctx->d_grad, &ctx->cap_grad, (size_t)nobj * 8, "rdc_backward: gradients"))
+        return st;
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_dl, dl_dimage, npix * 3 * sizeof(float), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    ctx->h2d_bytes += npix * 3 * sizeof(float);
+    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_grad, 0, (size_t)(nobj ? nobj : 1) * 8 * sizeof(float), ctx->stream));
+    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    ctx->last_launches = 0;
+    ctx->last_timed = false;
+    ctx->last_paths = npix * ctx->adj_n;
+    if (nobj > 0 && npix > 0) {
+        rdc::AdjParams p;
+        p.sc = ctx->view;
+        p.bvh = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
+        p.dl = ctx->d_dl;
+        p.grad = ctx->d_grad;
+        p.s0 = ctx->adj_s0;
+        p.nspp = ctx->adj_n;
+        p.max_bounces = ctx->adj_bounces;
+        p.stream_id = 0;
+        p.key0 = (uint32_t)ctx->adj_seed;
+        p.key1 = (uint32_t)(ctx->adj_seed >> 32);
+        p.npaths = (uint64_t)npix * ctx->adj_n;
+        p.segments = ctx->d_counters + 1;
+        const bool bvh = ctx->bvh_active;
+        if (!bvh && !ctx->brute_fits)
+            return fail(ctx, RDC_ERR_LIMIT, "rdc_backward: brute force needs the records in shared memory");
+        size_t smem = rdc::adjoint_smem_bytes(ctx->view, bvh, true);
+        p.smem_grad = smem <= kMaxSceneSmem ? 1u : 0u;
+        if (!p.smem_grad) smem = rdc::adjoint_smem_bytes(ctx->view, bvh, false);
+        const int block = rdc::kRenderBlock;
+        int per_sm = 0;
+        RDC_CUDA(ctx, rdc::adjoint_occupancy(bvh, block, smem, &per_sm));
+        if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_backward: scene does not fit in shared memory");
+        uint64_t grid = (uint64_t)ctx->num_sms * per_sm;
+        const uint64_t need = (p.npaths + block - 1) / block;
+        if (grid > need) grid = need;
+        RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+        RDC_CUDA(ctx, rdc::launch_adjoint(p, bvh, (int)grid, block, smem, ctx->stream));
+        RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+        ctx->last_timed = true;
+        ctx->last_launches = 1;
+    }
+    std::vector<float> g((size_t)nobj * 8);
+    if (nobj > 0) {
+        RDC_CUDA(ctx, cudaMemcpyAsync(g.data(), ctx->d_grad, g.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        ctx->d2h_bytes += g.size() * sizeof(float);
+    }
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (uint32_t j = 0; j < nobj; ++j) {
+        for (int c = 0; c < 3; ++c) {
+            if (grad_albedo) grad_albedo[3 * (size_t)j + c] = g[8 * (size_t)j + c];
+            if (grad_emission) grad_emission[3 * (size_t)j + c] = g[8 * (size_t)j + 3 + c];
+        }
+        // the kernels see roughness^2 (MatDev); d(r^2)/dr = 2r
+        if (grad_roughness)
+            grad_roughness[j] = g[8 * (size_t)j + 6] * 2.0f * ctx->host_objects[j].material.roughness;
+    }
     return RDC_OK;
 }
 

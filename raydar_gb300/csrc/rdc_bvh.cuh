@@ -128,8 +128,10 @@ struct BvhTrav {
     float3 oa, ob, inv;  // (o + m) / d, (o - m) / d per axis (m: see the file comment), 1/d
     float best;          // closest hit so far (+inf: none)
     int bidx;            // its object (-1: none)
-    int cur;             // next node to visit; -1 when the traversal is over
+    int cur;             // next node to visit; -1 when no node is left
     int sp;              // stack depth
+    int lnode;           // node whose leaf children in lmask are still to be tested
+    unsigned lmask;      // the traversal is over when cur < 0 and lmask == 0
 };
 
 constexpr int kBvhStack = 96;
@@ -150,6 +152,8 @@ __device__ __forceinline__ void bvh_begin(const BvhView& bv, const RayPre& r, bo
     T.bidx = -1;
     T.sp = 0;
     T.cur = -1;
+    T.lnode = 0;
+    T.lmask = 0u;
     if (bv.nobj == 0) return;
     if (bv.nobj == 1) {
         ++cnt.tests;
@@ -182,10 +186,11 @@ __device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb
     va = v;
 }
 
-// One node visit of a running traversal (T.cur >= 0): the four child boxes;
-// leaf children hit are tested at once; the nearest internal child hit is
-// visited next and the others pushed, farthest first; with none, the next
-// stacked box still in front of the best hit, or the end of the traversal
+// One node visit (T.cur >= 0, T.lmask == 0): the four child boxes; leaf
+// children hit are left in T.lmask for bvh_leaf_step (a warp tests them
+// together instead of one lane at a time inside the visit); the nearest
+// internal child hit is visited next and the others pushed, farthest first;
+// with none, the next stacked box still in front of the best hit, or none
 // (T.cur = -1).
 __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T,
                                          int* stack_node, float* stack_entry, BvhCounters& cnt) {
@@ -209,22 +214,14 @@ __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, boo
                     T.inv, limit, e[j]))
             hits |= 1u << j;
     }
-    unsigned leaves = hits & ((c[0] < 0 ? 1u : 0u) | (c[1] < 0 ? 2u : 0u) | (c[2] < 0 ? 4u : 0u) |
-                              (c[3] < 0 ? 8u : 0u));
-    while (leaves != 0u) {
-        const int j = __ffs(leaves) - 1;
-        leaves &= leaves - 1u;
-        const int cj = j == 0 ? c[0] : j == 1 ? c[1] : j == 2 ? c[2] : c[3];
-        ++cnt.tests;
-        bvh_leaf_any(bv, r, fast, ~cj, T.best, T.bidx);
-    }
-    // internal children still in front of the (possibly closer) best hit
-    const float lim = T.best * 1.0000038f + 1e-30f;
+    T.lmask = hits & ((c[0] < 0 ? 1u : 0u) | (c[1] < 0 ? 2u : 0u) | (c[2] < 0 ? 4u : 0u) | (c[3] < 0 ? 8u : 0u));
+    T.lnode = T.cur;
+    const float lim = limit;
     const float INF = __int_as_float(0x7f800000);
-    float k0 = ((hits & 1u) && c[0] >= 0 && e[0] <= lim) ? e[0] : INF;
-    float k1 = ((hits & 2u) && c[1] >= 0 && e[1] <= lim) ? e[1] : INF;
-    float k2 = ((hits & 4u) && c[2] >= 0 && e[2] <= lim) ? e[2] : INF;
-    float k3 = ((hits & 8u) && c[3] >= 0 && e[3] <= lim) ? e[3] : INF;
+    float k0 = ((hits & 1u) && c[0] >= 0) ? e[0] : INF;
+    float k1 = ((hits & 2u) && c[1] >= 0) ? e[1] : INF;
+    float k2 = ((hits & 4u) && c[2] >= 0) ? e[2] : INF;
+    float k3 = ((hits & 8u) && c[3] >= 0) ? e[3] : INF;
     int v0 = c[0], v1 = c[1], v2 = c[2], v3 = c[3];
     bvh_cswap(k0, v0, k1, v1);
     bvh_cswap(k2, v2, k3, v3);
@@ -262,6 +259,16 @@ __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, boo
     }
 }
 
+// Test the next pending leaf child (T.lmask != 0) of node T.lnode.
+__device__ __forceinline__ void bvh_leaf_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T,
+                                              BvhCounters& cnt) {
+    const int j = __ffs(T.lmask) - 1;
+    T.lmask &= T.lmask - 1u;
+    const int child = __float_as_int(__ldg(&bv.nodes[T.lnode].v[2 * j].w));
+    ++cnt.tests;
+    bvh_leaf_any(bv, r, fast, ~child, T.best, T.bidx);
+}
+
 // Closest hit through the BVH: the same (t, index) the brute-force loop gives.
 __device__ __forceinline__ void bvh_intersect(const BvhView& bv, const RayPre& r, bool fast, float& best, int& bidx,
                                               BvhCounters& cnt) {
@@ -269,7 +276,12 @@ __device__ __forceinline__ void bvh_intersect(const BvhView& bv, const RayPre& r
     float stack_entry[kBvhStack];
     BvhTrav T;
     bvh_begin(bv, r, fast, T, cnt);
-    while (T.cur >= 0) bvh_step(bv, r, fast, T, stack_node, stack_entry, cnt);
+    while (T.cur >= 0 || T.lmask != 0u) {
+        if (T.lmask != 0u)
+            bvh_leaf_step(bv, r, fast, T, cnt);
+        else
+            bvh_step(bv, r, fast, T, stack_node, stack_entry, cnt);
+    }
     best = T.best;
     bidx = T.bidx;
 }

@@ -377,21 +377,44 @@ __device__ __forceinline__ V3 unit_sphere(uint32_t a, uint32_t b, uint32_t c) {
     return vnormalize(mk(upm1(a), upm1(b), upm1(c)));
 }
 
+// What the adjoint needs to replay a scatter backwards: the lobe taken, the
+// diffuse flip, the transmission offset, the |dir| < 1e-5 fallback, and the
+// unit-sphere vector the lobe added (scaled by roughness^2).
+enum : uint32_t {
+    kLobeDiffuse = 0u,
+    kLobeSpecular = 1u,
+    kLobeRefract = 2u,
+    kScatFlip = 4u,      // diffuse = -(n + s1)
+    kScatTrans = 8u,     // transmission ray: origin offset along the new direction
+    kScatNormal = 16u,   // |dir|^2 < 1e-10: the new direction is the normal
+    kScatFront = 32u,    // the hit's front-face flag
+};
+struct ScatterRec {
+    uint32_t flags;
+    V3 s;
+};
+
 // The hit branch of per_pixel (src/renderer/cpu.rs:262-328): new ray from a
-// hit, the object's material and the bounce's random words w[0..10].
-__device__ __forceinline__ void scatter(V3 d, const HitRec& h, const MatDev& m,
-                                        const uint32_t* w, V3& o_out, V3& d_out) {
+// hit, the object's material and the bounce's random words w[0..10].  With
+// Rec, also fills *rec; the arithmetic is the same either way.
+template <bool Rec>
+__device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev& m, const uint32_t* w, V3& o_out,
+                                             V3& d_out, ScatterRec* rec) {
     const float rough = m.a.w;
     const float metallic = m.b.w;
     const float transmission = m.c.x;
 
     V3 diffuse = vadd(h.n, unit_sphere(w[0], w[1], w[2]));
-    if (vdot(diffuse, h.n) < 0.0f) diffuse = vneg(diffuse);
+    const bool flip = vdot(diffuse, h.n) < 0.0f;
+    if (flip) diffuse = vneg(diffuse);
 
     // reflect, src/utils/mod.rs:14-16: v - n * (v.n) * 2
     const float dn = vdot(d, h.n);
     const V3 perfect = vsub(d, vmul(vmul(h.n, dn), 2.0f));
-    const V3 specular = vnormalize(vadd(perfect, vmul(unit_sphere(w[3], w[4], w[5]), rough)));
+    const V3 s2 = unit_sphere(w[3], w[4], w[5]);
+    const V3 specular = vnormalize(vadd(perfect, vmul(s2, rough)));
+    uint32_t lobe = kLobeSpecular;
+    V3 s_used = s2;
 
     const bool trans = u01(w[6]) < transmission;
     V3 dir;
@@ -416,7 +439,10 @@ __device__ __forceinline__ void scatter(V3 d, const HitRec& h, const MatDev& m,
             const V3 perp = vmul(vadd(rd, vmul(h.n, cos_theta)), ratio);
             const float s = -sqrtf(fabsf(1.0f - vdot(perp, perp)));
             const V3 rf = vadd(perp, vmul(h.n, s));
-            dir = vnormalize(vadd(rf, vmul(unit_sphere(w[8], w[9], w[10]), rough)));
+            const V3 s3 = unit_sphere(w[8], w[9], w[10]);
+            dir = vnormalize(vadd(rf, vmul(s3, rough)));
+            lobe = kLobeRefract;
+            s_used = s3;
         } else {
             dir = specular;
         }
@@ -424,12 +450,24 @@ __device__ __forceinline__ void scatter(V3 d, const HitRec& h, const MatDev& m,
         dir = specular;
     } else if (u01(w[8]) < rough) {
         dir = diffuse;
+        lobe = kLobeDiffuse;
     } else {
         dir = specular;
     }
     const V3 off = trans ? dir : h.n;
     o_out = vadd(h.p, vmul(off, 0.0001f));
-    d_out = vdot(dir, dir) < 1e-10f ? h.n : dir;
+    const bool to_normal = vdot(dir, dir) < 1e-10f;
+    d_out = to_normal ? h.n : dir;
+    if (Rec) {
+        rec->flags = lobe | (flip ? kScatFlip : 0u) | (trans ? kScatTrans : 0u) | (to_normal ? kScatNormal : 0u) |
+                     (h.front ? kScatFront : 0u);
+        rec->s = s_used;
+    }
+}
+
+__device__ __forceinline__ void scatter(V3 d, const HitRec& h, const MatDev& m, const uint32_t* w, V3& o_out,
+                                        V3& d_out) {
+    scatter_impl<false>(d, h, m, w, o_out, d_out, nullptr);
 }
 
 // World::sample, src/scene/world.rs:17-31 (the dot with +Y is d.x*0 + d.y*1 + d.z*0).

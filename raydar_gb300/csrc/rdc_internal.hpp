@@ -98,6 +98,23 @@ struct RenderParams {
     uint32_t min_idle;                // render_bvh_kernel: lanes done before a warp shades
 };
 
+// Path-replay adjoint (rdc_adjoint.cu).  grad holds 8 floats per object:
+// dL/dalbedo (3), dL/demission (3), dL/d(roughness^2), unused.
+constexpr uint32_t kAdjMaxBounces = 16;
+struct AdjParams {
+    SceneView sc;
+    BvhView bvh;        // used when the scene has an LBVH
+    const float* dl;    // dL/dimage, npix * 3 (RGB of the mean-radiance image)
+    float* grad;        // nobj * 8, zeroed by the caller
+    uint32_t s0, nspp, max_bounces, stream_id, key0, key1;
+    uint64_t npaths;    // npix * nspp
+    unsigned long long* segments;
+    uint32_t smem_grad; // 1: per-block shared accumulators (8 * nobj floats)
+};
+size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad);
+cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, size_t smem, cudaStream_t s);
+
 // One scene of a batch (rdc_batch_upload): its view, accumulator, sample
 // count, bounce limit, RNG key and share of the batch's estimated work.
 struct BatchScene {

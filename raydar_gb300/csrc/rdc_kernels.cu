@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
 
     for (;;) {
         // Shade the lanes whose traversal is over and start their next segment.
-        if (in_flight && T.cur < 0) {
+        if (in_flight && T.cur < 0 && T.lmask == 0u) {
             const bool ended = segment_shade(P.sc, st, T.best, T.bidx, (uint32_t)pix, sample, P.max_bounces,
                                              P.stream_id, P.key0, P.key1);
             advance(ended);
@@ -202,12 +202,20 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
             }
         }
         if (__ballot_sync(FULL, pix >= 0) == 0u) break;
-        // Traversal steps until min_idle lanes are done (at least one step).
-        unsigned act = __ballot_sync(FULL, in_flight && T.cur >= 0);
-        while (act != 0u) {
-            if (in_flight && T.cur >= 0) bvh_step(P.bvh, r, rfast, T, stack_node, stack_entry, cnt);
-            act = __ballot_sync(FULL, in_flight && T.cur >= 0);
-            if (32u - (unsigned)__popc(act) >= P.min_idle) break;
+        // Traversal until min_idle lanes are done (at least one step).  Each
+        // step is a node visit for the lanes without pending leaves, or a
+        // leaf test for the lanes with some, whichever more lanes wait for.
+        for (bool first = true;; first = false) {
+            const bool wl = in_flight && T.lmask != 0u;
+            const bool wn = in_flight && T.lmask == 0u && T.cur >= 0;
+            const unsigned lm = __ballot_sync(FULL, wl), nm = __ballot_sync(FULL, wn);
+            const unsigned act = lm | nm;
+            if (act == 0u || (!first && 32u - (unsigned)__popc(act) >= P.min_idle)) break;
+            if (__popc(lm) >= __popc(nm)) {
+                if (wl) bvh_leaf_step(P.bvh, r, rfast, T, cnt);
+            } else {
+                if (wn) bvh_step(P.bvh, r, rfast, T, stack_node, stack_entry, cnt);
+            }
         }
     }
     add_warp_sum(P.segments, segs);

@@ -114,6 +114,8 @@ SIGNATURES = {
     "rdc_batch_set_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
     "rdc_batch_get_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
     "rdc_set_render_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
+    "rdc_forward": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _FP]),
+    "rdc_backward": (C.c_int, [_P, _FP, _FP, _FP, _FP]),
     "rdc_get_render_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
     "rdc_batch_autotune": (C.c_int, [_P, C.POINTER(RdcLaunchConfig), C.POINTER(C.c_float)]),
     "rdc_write_accum": (C.c_int, [_P, _FP, C.c_size_t, C.c_uint32]),

@@ -99,7 +99,9 @@ class CudaRenderer:
     def upload(self, scene: Scene, force: bool = False):
         """Copy the scene to the device if it changed since the last call."""
         sc = scene.to_c()
-        key = bytes(sc.desc) + bytes(sc.objects)
+        # the descriptor's objects pointer differs per to_c(): compare contents
+        key = bytes(sc.desc.camera) + bytes(sc.desc.world) + bytes(sc.objects)[: sc.desc.object_count *
+                                                                                C.sizeof(native.RdcObject)]
         if force or key != self._uploaded:
             self._check(self.lib.rdc_scene_upload(self.ctx, sc.ref()), "rdc_scene_upload")
             self._uploaded = key
@@ -124,6 +126,28 @@ class CudaRenderer:
         s = native.RdcStats()
         self._check(self.lib.rdc_stats_get(self.ctx, C.byref(s)), "rdc_stats_get")
         return s
+
+    # ------------------------------------------------------ differentiation --
+    def forward(self, scene: Scene, spp: int, spp_begin: int = 0) -> np.ndarray:
+        """Mean-radiance image (H x W x 3) of samples [spp_begin, spp_begin+spp)
+        with the configured bounce limit and seed (rdc_forward)."""
+        self.upload(scene)
+        out = np.empty((scene.height, scene.width, 3), np.float32)
+        self._check(self.lib.rdc_forward(self.ctx, spp_begin, spp, self.config.max_bounces, self.seed,
+                                         native.fptr(out)), "rdc_forward")
+        return out
+
+    def backward(self, scene: Scene, dl_dimage: np.ndarray):
+        """(dL/dalbedo N x 3, dL/droughness N, dL/demission N x 3) for the image
+        of the last forward(), given dL/dimage (H x W x 3) (rdc_backward)."""
+        n = int(self._scene_c.desc.object_count) if self._scene_c is not None else len(scene.objects)
+        dl = np.ascontiguousarray(dl_dimage, np.float32).reshape(scene.height, scene.width, 3)
+        ga = np.zeros((n, 3), np.float32)
+        gr = np.zeros(n, np.float32)
+        ge = np.zeros((n, 3), np.float32)
+        self._check(self.lib.rdc_backward(self.ctx, native.fptr(dl), native.fptr(ga), native.fptr(gr),
+                                          native.fptr(ge)), "rdc_backward")
+        return ga, gr, ge
 
     # ----------------------------------------------------- trait Renderer --
     def render_frame(self, scene: Scene) -> np.ndarray:
