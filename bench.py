@@ -58,6 +58,8 @@ def _args():
     p.add_argument("--no-batch", action="store_true", help="skip the batched (config 3) measurement")
     p.add_argument("--batch-only", action="store_true", help="only the batched (config 3) measurement")
     p.add_argument("--no-large", action="store_true", help="skip the LBVH (config 5) measurement")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (config 4) measurement")
+    p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
     p.add_argument("--batch-spp-div", type=int, default=1, help="divide every batch item's spp (small profiling case)")
     return p.parse_args()
 
@@ -332,6 +334,110 @@ def lbvh_bench(local: int, steps: int, peak_tflops: float):
     }
 
 
+def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
+    """Config 4: 512x512, 128 spp, 6 bounces, 32 spheres + 2 emissive spheres
+    + ground.  Loss = L2 distance to a target rendered from the same scene with
+    every parameter perturbed by N(0, 0.05) and clamped (albedo and roughness
+    to [0, 1], emission >= 0).  Per step: rdc_forward, then rdc_backward with
+    dL/dimage = 2 (image - target); device times of both kernels and their
+    ratio.  Then central differences with common random numbers (same seed,
+    eps 1e-3, fd_spp samples) for two albedo channels and one emission,
+    against the adjoint at the same spp."""
+    import copy
+
+    import numpy as np
+
+    from raydar_gb300 import CudaRenderer, RendererConfig, scenegen
+
+    w = scenegen.c4_diff()
+    scene = w.scene
+    rng = np.random.default_rng(40)
+    target_scene = copy.deepcopy(scene)
+    for o in target_scene.objects:
+        m = o.material
+        m.albedo = np.clip(m.albedo + rng.normal(0, 0.05, 3), 0, 1).astype(np.float32)
+        m.roughness = float(np.float32(np.clip(m.roughness + rng.normal(0, 0.05), 0, 1)))
+        if m.emission_strength > 0:
+            m.emission_strength = float(np.float32(max(m.emission_strength + rng.normal(0, 0.05), 0.0)))
+    r = CudaRenderer(RendererConfig(max_bounces=w.max_bounces), device=local, seed=11)
+    target = r.forward(target_scene, w.spp)
+    r.forward(scene, w.spp)  # warm-up
+    fwd_ms, bwd_ms, fwd_segs, bwd_segs = [], [], 0, 0
+    t0 = time.perf_counter()
+    for k in range(steps):
+        r.seed = 500 + k
+        img = r.forward(scene, w.spp)
+        st = r.stats()
+        fwd_ms.append(st.device_ms)
+        fwd_segs += st.segments
+        dl = 2.0 * (img - target)
+        ga, gr, ge = r.backward(scene, dl)
+        st = r.stats()
+        bwd_ms.append(st.device_ms)
+        bwd_segs += st.segments
+    wall = time.perf_counter() - t0
+
+    # central differences with common random numbers at fd_spp
+    r.seed = 77
+    img = r.forward(scene, fd_spp)
+    dl = 2.0 * (img - target)
+    ga, gr, ge = r.backward(scene, dl)
+
+    def loss(s):
+        r.seed = 77
+        im = r.forward(s, fd_spp)
+        return float(((im.astype(np.float64) - target) ** 2).sum())
+
+    checks = []
+    diffuse = next(i for i, o in enumerate(scene.objects) if i > 0 and o.material.roughness == 1.0
+                   and o.material.emission_strength == 0)
+    for j, c in ((0, 1), (diffuse, 0)):
+        lo, hi = copy.deepcopy(scene), copy.deepcopy(scene)
+        lo.objects[j].material.albedo = lo.objects[j].material.albedo.copy()
+        hi.objects[j].material.albedo = hi.objects[j].material.albedo.copy()
+        a = float(scene.objects[j].material.albedo[c])
+        lo.objects[j].material.albedo[c] = np.float32(a - 1e-3)
+        hi.objects[j].material.albedo[c] = np.float32(a + 1e-3)
+        den = float(hi.objects[j].material.albedo[c]) - float(lo.objects[j].material.albedo[c])
+        fd = (loss(hi) - loss(lo)) / den
+        checks.append({"param": f"albedo[{j}][{c}]", "adjoint": float(ga[j, c]), "central_difference": fd,
+                       "rel_gap": float(abs(fd - ga[j, c]) / max(abs(fd), 1e-30))})
+    j = len(scene.objects) - 1
+    lo, hi = copy.deepcopy(scene), copy.deepcopy(scene)
+    s0 = scene.objects[j].material.emission_strength
+    lo.objects[j].material.emission_strength = float(np.float32(s0 - 1e-3))
+    hi.objects[j].material.emission_strength = float(np.float32(s0 + 1e-3))
+    den = hi.objects[j].material.emission_strength - lo.objects[j].material.emission_strength
+    fd = float((loss(hi) - loss(lo)) / den)
+    adj = float((ge[j] * np.asarray(scene.objects[j].material.emission_color, np.float32)).sum())
+    checks.append({"param": f"emission_strength[{j}]", "adjoint": adj, "central_difference": fd,
+                   "rel_gap": abs(fd - adj) / max(abs(fd), 1e-30)})
+    # roughness: the difference quotient also holds the paths whose hit or lobe
+    # flips within the step, which path replay leaves out (a stated gap)
+    metals = [i for i, o in enumerate(scene.objects) if o.material.metallic == 1.0 and o.material.roughness > 0.1]
+    j = max(metals, key=lambda i: abs(gr[i]))
+    lo, hi = copy.deepcopy(scene), copy.deepcopy(scene)
+    r0 = scene.objects[j].material.roughness
+    lo.objects[j].material.roughness = float(np.float32(r0 - 1e-3))
+    hi.objects[j].material.roughness = float(np.float32(r0 + 1e-3))
+    den = hi.objects[j].material.roughness - lo.objects[j].material.roughness
+    fd = float((loss(hi) - loss(lo)) / den)
+    checks.append({"param": f"roughness[{j}]", "adjoint": float(gr[j]), "central_difference": fd,
+                   "rel_gap": abs(fd - float(gr[j])) / max(abs(fd), 1e-30),
+                   "note": "difference includes hit/lobe changes that path replay omits"})
+    r.close()
+    f_ms, b_ms = sum(fwd_ms) / steps, sum(bwd_ms) / steps
+    return {
+        "workload": "c4_diff: 512x512, 128 spp, 6 bounces, 32 spheres + 2 emissive + ground; L2 loss to a "
+                    "perturbed-parameter target",
+        "forward_ms": f_ms, "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+        "forward_segments_per_s": fwd_segs / (sum(fwd_ms) / 1e3),
+        "backward_replayed_segments_per_s": bwd_segs / (sum(bwd_ms) / 1e3),
+        "steps": steps, "wall_s": wall,
+        "fd_check": {"spp": fd_spp, "eps": 1e-3, "common_random_numbers": True, "params": checks},
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -455,6 +561,10 @@ def run_ours(args):
         pk = max(ops_s.value / 1e12, n_sms * 128 * (clk.get("sm_mhz") or 0.0) * 1e6 / 1e12)
         large = lbvh_bench(local, max(1, min(args.steps, 2)), pk)
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = adjoint_bench(local, max(1, min(args.steps, 3)))
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -502,6 +612,7 @@ def run_ours(args):
         "cpu_baseline": base,
         "batched": batched,
         "large_scene": large,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
 
@@ -512,6 +623,11 @@ def main():
         import torch
         torch.cuda.set_device(_dist()[2])
         print(json.dumps({"batched": batch_bench(_dist()[2], max(1, min(args.steps, 3)), args.batch_spp_div)}))
+        return
+    if args.adjoint_only:
+        import torch
+        torch.cuda.set_device(_dist()[2])
+        print(json.dumps({"adjoint": adjoint_bench(_dist()[2], max(1, min(args.steps, 3)))}))
         return
     if args.impl == "reference":
         run_reference(args)
