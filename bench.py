@@ -60,6 +60,8 @@ def _args():
     p.add_argument("--no-large", action="store_true", help="skip the LBVH (config 5) measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (config 4) measurement")
     p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
+    p.add_argument("--inverse", action="store_true",
+                   help="only the config 5 inverse-rendering run (200 Adam steps on 1000 albedos)")
     p.add_argument("--batch-spp-div", type=int, default=1, help="divide every batch item's spp (small profiling case)")
     return p.parse_args()
 
@@ -69,6 +71,20 @@ def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def combine_replicas(dist, elapsed_s: float, segments: float, device: str):
+    """Replicas only: every rank renders its own frames, with no exchange on
+    the data path.  Whole-job figures are the slowest rank's time and the sum
+    of all ranks' segments.  dist = None on one rank."""
+    if dist is None:
+        return float(elapsed_s), float(segments)
+    import torch
+    t = torch.tensor([float(elapsed_s)], dtype=torch.float64, device=device)
+    s = torch.tensor([float(segments)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(s, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(s.item())
 
 
 def _workload():
@@ -438,6 +454,76 @@ def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
     }
 
 
+def inverse_bench(local: int, steps: int = 200, lr: float = 1e-2, spp: int = 64):
+    """Config 5, inverse: recover the albedos of the 1,000 spheres nearest the
+    camera in the 100k-sphere / 10k-cube scene (device LBVH) from a 512x512,
+    64 spp target.  Start from albedo 0.5 for those spheres; each step renders
+    (rdc_forward, fresh seed), takes the L2 loss to the target, runs
+    rdc_backward and applies Adam (lr 1e-2) to their albedos, clamped to
+    [0, 1], written back with rdc_update_materials (no geometry upload, no
+    LBVH rebuild).  Reports the recovered-parameter RMSE before and after."""
+    import numpy as np
+
+    from raydar_gb300 import CudaRenderer, RendererConfig, scenegen
+    from raydar_gb300.scene import material_records
+
+    w = scenegen.c5_large(width=512, height=512)
+    scene = w.scene
+    rec = scene.packed
+    cam = np.asarray(scene.camera.position, np.float64)
+    spheres = np.where(rec["geometry"] == 0)[0]
+    dist = np.linalg.norm(rec["center"][spheres].astype(np.float64) - cam, axis=1)
+    chosen = spheres[np.argsort(dist)[:1000]]
+    truth = rec["albedo"][chosen].astype(np.float64)
+
+    r = CudaRenderer(RendererConfig(max_bounces=w.max_bounces), device=local, seed=1)
+    t0 = time.perf_counter()
+    r.upload(scene)
+    r.seed = 900
+    target = r.forward(None, 4 * spp)  # a cleaner target than one step's estimate
+    mats = material_records(scene)
+    est = np.full_like(truth, 0.5)
+    mats["albedo"][chosen] = est.astype(np.float32)
+    r.update_materials(mats)
+    rmse0 = float(np.sqrt(((est - truth) ** 2).mean()))
+    m1 = np.zeros_like(est)
+    m2 = np.zeros_like(est)
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    fwd_ms = bwd_ms = 0.0
+    losses = []
+    for k in range(steps):
+        r.seed = 1000 + k
+        img = r.forward(None, spp)
+        fwd_ms += r.stats().device_ms
+        diff = img.astype(np.float64) - target
+        losses.append(float((diff ** 2).sum()))
+        ga, _, _ = r.backward(None, (2.0 * diff).astype(np.float32))
+        bwd_ms += r.stats().device_ms
+        g = ga[chosen].astype(np.float64)
+        m1 = b1 * m1 + (1 - b1) * g
+        m2 = b2 * m2 + (1 - b2) * g * g
+        mh = m1 / (1 - b1 ** (k + 1))
+        vh = m2 / (1 - b2 ** (k + 1))
+        est = np.clip(est - lr * mh / (np.sqrt(vh) + eps), 0.0, 1.0)
+        mats["albedo"][chosen] = est.astype(np.float32)
+        r.update_materials(mats)
+    wall = time.perf_counter() - t0
+    st = r.stats()
+    r.close()
+    seen = np.abs(est - 0.5).sum(axis=1) > 0  # spheres whose albedo moved (seen by some path)
+    return {
+        "workload": "c5_large at 512x512: 100k spheres + 10k cubes, device LBVH; albedos of the 1000 spheres "
+                    f"nearest the camera from a {4 * spp} spp target, {spp} spp per step",
+        "steps": steps, "lr": lr, "optimizer": "Adam(0.9, 0.999)",
+        "rmse_initial": rmse0, "rmse_final": float(np.sqrt(((est - truth) ** 2).mean())),
+        "rmse_final_spheres_moved": float(np.sqrt(((est[seen] - truth[seen]) ** 2).mean())) if seen.any() else None,
+        "spheres_moved": int(seen.sum()),
+        "loss_first": losses[0], "loss_last": losses[-1],
+        "forward_ms_per_step": fwd_ms / steps, "backward_ms_per_step": bwd_ms / steps,
+        "wall_s": wall, "accel": int(st.accel),
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -517,15 +603,7 @@ def run_ours(args):
     kernel_ms = [a.elapsed_time(b) for a, b in evs]
     my_segments = sum(segs)
 
-    if dist is not None:
-        t = torch.tensor([elapsed], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-        s = torch.tensor([my_segments], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(s, op=dist.ReduceOp.SUM)
-        total_segments = float(s.item())
-    else:
-        total_segments = float(my_segments)
+    elapsed, total_segments = combine_replicas(dist, elapsed, my_segments, f"cuda:{local}")
 
     # ---- e2e through the C ABI from host buffers --------------------------
     img = np.empty((w.scene.height, w.scene.width, 4), np.uint8)
@@ -542,15 +620,7 @@ def run_ours(args):
         e2e_segs += r.stats().segments
     te1 = time.perf_counter()
     st1 = r.stats()
-    e2e_time = te1 - te0
-    if dist is not None:
-        t = torch.tensor([e2e_time, float(e2e_segs)], dtype=torch.float64, device=f"cuda:{local}")
-        tm = t.clone()
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e_time, e2e_total = float(tm[0].item()), float(t[1].item())
-    else:
-        e2e_total = float(e2e_segs)
+    e2e_time, e2e_total = combine_replicas(dist, te1 - te0, e2e_segs, f"cuda:{local}")
 
     batched = None
     if rank == 0 and not args.no_batch:
@@ -623,6 +693,11 @@ def main():
         import torch
         torch.cuda.set_device(_dist()[2])
         print(json.dumps({"batched": batch_bench(_dist()[2], max(1, min(args.steps, 3)), args.batch_spp_div)}))
+        return
+    if args.inverse:
+        import torch
+        torch.cuda.set_device(_dist()[2])
+        print(json.dumps({"inverse": inverse_bench(_dist()[2])}))
         return
     if args.adjoint_only:
         import torch

@@ -176,6 +176,13 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* scene);
  * reference always tests every object (src/renderer/cpu.rs:344-352). */
 rdc_status rdc_set_accel(rdc_ctx* ctx, uint32_t mode);
 
+/* Replace the materials of the uploaded scene's objects (count = its object
+ * count, in scene order) without re-uploading geometry or rebuilding the
+ * LBVH: the per-step update of an inverse-rendering loop, or of the editor's
+ * material inspector (src/widgets/inspector.rs:433-531).  The accumulator is
+ * kept; a later rdc_backward needs a new rdc_forward. */
+rdc_status rdc_update_materials(rdc_ctx* ctx, const rdc_material* materials, uint32_t count);
+
 /* ---- rendering -------------------------------------------------------- */
 
 /* Zero the RGBA accumulator and the sample count: Renderer::new_frame

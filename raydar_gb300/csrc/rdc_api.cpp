@@ -376,6 +376,29 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     return RDC_OK;
 }
 
+rdc_status rdc_update_materials(rdc_ctx* ctx, const rdc_material* materials, uint32_t count) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_update_materials: no scene uploaded");
+    const uint32_t n = ctx->host_desc.object_count;
+    if (count != n)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_update_materials: count differs from the scene's object count");
+    if (n == 0) return RDC_OK;
+    if (!materials) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_update_materials: materials is NULL");
+    if (rdc_status st = set_device(ctx)) return st;
+    std::vector<MatDev> mat(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        ctx->host_objects[i].material = materials[i];
+        mat[i] = rdc::flat_material(ctx->host_objects[i]);
+    }
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // no kernel may read mat[] while it changes
+    RDC_CUDA(ctx, cudaMemcpyAsync(ctx->d_mat, mat.data(), mat.size() * sizeof(MatDev), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->h2d_bytes += mat.size() * sizeof(MatDev);
+    ctx->adj_valid = false;
+    return RDC_OK;
+}
+
 rdc_status rdc_set_accel(rdc_ctx* ctx, uint32_t mode) {
     if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
     if (mode > RDC_ACCEL_LBVH) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_set_accel: unknown mode");

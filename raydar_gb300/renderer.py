@@ -127,21 +127,39 @@ class CudaRenderer:
         self._check(self.lib.rdc_stats_get(self.ctx, C.byref(s)), "rdc_stats_get")
         return s
 
+    def update_materials(self, materials: np.ndarray):
+        """Replace the uploaded scene's materials (MATERIAL_DTYPE records, scene
+        order) without re-uploading geometry (rdc_update_materials)."""
+        from .scene import MATERIAL_DTYPE
+        m = np.ascontiguousarray(materials, MATERIAL_DTYPE)
+        self._check(self.lib.rdc_update_materials(self.ctx, m.ctypes.data_as(C.POINTER(native.RdcMaterial)),
+                                                  len(m)), "rdc_update_materials")
+        self._uploaded = None  # the cached scene no longer matches the device copy
+
     # ------------------------------------------------------ differentiation --
-    def forward(self, scene: Scene, spp: int, spp_begin: int = 0) -> np.ndarray:
+    def _dims(self):
+        c = self._scene_c.desc.camera
+        return int(c.resolution_y), int(c.resolution_x), int(self._scene_c.desc.object_count)
+
+    def forward(self, scene: Optional[Scene], spp: int, spp_begin: int = 0) -> np.ndarray:
         """Mean-radiance image (H x W x 3) of samples [spp_begin, spp_begin+spp)
-        with the configured bounce limit and seed (rdc_forward)."""
-        self.upload(scene)
-        out = np.empty((scene.height, scene.width, 3), np.float32)
+        with the configured bounce limit and seed (rdc_forward).  scene None:
+        the scene on the device as it is (e.g. after update_materials)."""
+        if scene is not None:
+            self.upload(scene)
+        h, w, _ = self._dims()
+        out = np.empty((h, w, 3), np.float32)
         self._check(self.lib.rdc_forward(self.ctx, spp_begin, spp, self.config.max_bounces, self.seed,
                                          native.fptr(out)), "rdc_forward")
         return out
 
-    def backward(self, scene: Scene, dl_dimage: np.ndarray):
+    def backward(self, scene: Optional[Scene], dl_dimage: np.ndarray):
         """(dL/dalbedo N x 3, dL/droughness N, dL/demission N x 3) for the image
         of the last forward(), given dL/dimage (H x W x 3) (rdc_backward)."""
-        n = int(self._scene_c.desc.object_count) if self._scene_c is not None else len(scene.objects)
-        dl = np.ascontiguousarray(dl_dimage, np.float32).reshape(scene.height, scene.width, 3)
+        if self._scene_c is None:
+            raise native.RdcError(4, "backward: no scene uploaded")  # RDC_ERR_NO_SCENE
+        h, w, n = self._dims()
+        dl = np.ascontiguousarray(dl_dimage, np.float32).reshape(h, w, 3)
         ga = np.zeros((n, 3), np.float32)
         gr = np.zeros(n, np.float32)
         ge = np.zeros((n, 3), np.float32)

@@ -304,6 +304,25 @@ OBJECT_DTYPE = np.dtype([
 ])
 assert OBJECT_DTYPE.itemsize == C.sizeof(native.RdcObject)
 
+MATERIAL_FIELDS = ("albedo", "roughness", "metallic", "emission_color", "emission_strength", "transmission", "ior")
+MATERIAL_DTYPE = np.dtype([(f, OBJECT_DTYPE.fields[f][0]) for f in MATERIAL_FIELDS])
+assert MATERIAL_DTYPE.itemsize == C.sizeof(native.RdcMaterial)
+
+
+def material_records(scene) -> np.ndarray:
+    """The objects' materials as rdc_material records (MATERIAL_DTYPE), in scene order."""
+    if isinstance(scene, PackedScene):
+        src = scene.packed
+        out = np.empty(len(src), MATERIAL_DTYPE)
+        for f in MATERIAL_FIELDS:
+            out[f] = src[f]
+        return out
+    out = np.empty(len(scene.objects), MATERIAL_DTYPE)
+    for i, o in enumerate(scene.objects):
+        m = o.material
+        out[i] = (m.albedo, m.roughness, m.metallic, m.emission_color, m.emission_strength, m.transmission, m.ior)
+    return out
+
 
 class PackedScene(Scene):
     """A Scene whose objects live in one numpy array of OBJECT_DTYPE records

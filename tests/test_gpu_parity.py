@@ -29,10 +29,32 @@ def _render_gpu(r, scene, s0, n, bounces, seed):
     return acc, r.stats().segments
 
 
+def _ortho(scene, size):
+    """The same scene seen through Projection::Orthographic (src/scene/camera.rs:8-11, 218-225)."""
+    import copy
+    s = copy.deepcopy(scene)
+    s.camera.projection = "Orthographic"
+    s.camera.size = float(np.float32(size))
+    s.camera.update_matrices()
+    return s
+
+
+def _solid(scene):
+    """World::SolidColor (src/scene/world.rs:6-14, 31)."""
+    import copy
+
+    from raydar_gb300.scene import World
+    s = copy.deepcopy(scene)
+    s.world = World("SolidColor", color=np.array([0.25, 0.5, 0.75], np.float32))
+    return s
+
+
 SCENES = {
     "c1_64x36": lambda: shrink(scenegen.c1_plain().scene, 64, 36),
     "c2_96x54": lambda: shrink(scenegen.c2_default().scene, 96, 54),
     "c4_48x48": lambda: shrink(scenegen.c4_diff().scene, 48, 48),
+    "c2_ortho_96x54": lambda: _ortho(shrink(scenegen.c2_default().scene, 96, 54), 14.0),
+    "c1_solid_world_64x36": lambda: _solid(shrink(scenegen.c1_plain().scene, 64, 36)),
 }
 
 
