@@ -58,6 +58,8 @@ def _args():
     p.add_argument("--no-batch", action="store_true", help="skip the batched (config 3) measurement")
     p.add_argument("--batch-only", action="store_true", help="only the batched (config 3) measurement")
     p.add_argument("--no-large", action="store_true", help="skip the LBVH (config 5) measurement")
+    p.add_argument("--large-only", default="", metavar="WxHxSPP",
+                   help="only the LBVH (config 5) measurement, at WxHxSPP (e.g. 480x270x32; 0 = full size)")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (config 4) measurement")
     p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
     p.add_argument("--inverse", action="store_true",
@@ -299,14 +301,17 @@ def batch_bench(local: int, steps: int, spp_div: int = 1):
     }
 
 
-def lbvh_bench(local: int, steps: int, peak_tflops: float):
+def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, height: int = 1080, spp: int = 0):
     """Config 5 forward: 100k spheres + 10k cubes, device-built LBVH, one
-    1920x1080 frame of 256 spp / 12 bounces per step.  Ops/segment follow the
-    LBVH model 30 * node visits + 24 * object tests + 100, with the visit and
-    test counts measured by the kernel in the same launches."""
+    1920x1080 frame of 256 spp / 12 bounces per step (width, height, spp:
+    a smaller case of the same scene).  Ops/segment follow the LBVH model
+    30 * node visits + 24 * object tests + 100, with the visit and test counts
+    measured by the kernel in the same launches."""
     from raydar_gb300 import CudaRenderer, RendererConfig, native, scenegen
 
-    w = scenegen.c5_large()
+    w = scenegen.c5_large(width=width, height=height)
+    if spp:
+        w.spp = spp
     r = CudaRenderer(RendererConfig(max_sample_count=w.spp, max_bounces=w.max_bounces), device=local, seed=0)
     t0 = time.perf_counter()
     r.upload(w.scene)
@@ -336,7 +341,7 @@ def lbvh_bench(local: int, steps: int, peak_tflops: float):
     achieved = ops * segs / (dev_ms / 1e3) / 1e12
     return {
         "workload": "c5_large: 100k spheres r in [0.01,0.2] + 10k cubes edge in [0.02,0.3] in a 40x10x40 box, "
-                    "1920x1080, 256 spp, 12 bounces, device-built LBVH",
+                    f"{width}x{height}, {w.spp} spp, 12 bounces, device-built LBVH",
         "segments_per_s": segs / wall,
         "kernel_ms_per_frame": dev_ms / steps,
         "node_visits_per_segment": v_per,
@@ -693,6 +698,12 @@ def main():
         import torch
         torch.cuda.set_device(_dist()[2])
         print(json.dumps({"batched": batch_bench(_dist()[2], max(1, min(args.steps, 3)), args.batch_spp_div)}))
+        return
+    if args.large_only:
+        import torch
+        torch.cuda.set_device(_dist()[2])
+        wh = [int(x) for x in args.large_only.split("x")] if args.large_only != "0" else [1920, 1080, 0]
+        print(json.dumps({"large_scene": lbvh_bench(_dist()[2], max(1, min(args.steps, 2)), 0.0, *wh)}))
         return
     if args.inverse:
         import torch
