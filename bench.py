@@ -62,6 +62,8 @@ def _args():
                    help="only the LBVH (config 5) measurement, at WxHxSPP (e.g. 480x270x32; 0 = full size)")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (config 4) measurement")
     p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
+    p.add_argument("--no-wavefront", action="store_true", help="skip the megakernel / wavefront A/B")
+    p.add_argument("--wavefront-only", action="store_true", help="only the megakernel / wavefront A/B")
     p.add_argument("--inverse", action="store_true",
                    help="only the config 5 inverse-rendering run (200 Adam steps on 1000 albedos)")
     p.add_argument("--batch-spp-div", type=int, default=1, help="divide every batch item's spp (small profiling case)")
@@ -459,6 +461,39 @@ def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
     }
 
 
+def wavefront_bench(local: int, steps: int, spp: int = 64):
+    """Megakernel vs wavefront A/B on the headline scene (c2_default 1920x1080,
+    12 bounces) at `spp` samples per frame: the same paths, the same
+    accumulator bit for bit; device time of each form."""
+    from raydar_gb300 import CudaRenderer, RendererConfig, scenegen
+
+    w = scenegen.c2_default()
+    out = {}
+    for fn in ("rdc_render", "rdc_render_wavefront"):
+        r = CudaRenderer(RendererConfig(max_bounces=w.max_bounces), device=local, seed=0)
+        r.upload(w.scene)
+        f = getattr(r.lib, fn)
+        r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+        r._check(f(r.ctx, 0, spp, w.max_bounces, 1), fn)  # warm-up
+        r.stats()
+        ms, segs = 0.0, 0
+        for k in range(steps):
+            r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+            r._check(f(r.ctx, 0, spp, w.max_bounces, 100 + k), fn)
+            st = r.stats()
+            ms += st.device_ms
+            segs += st.segments
+        r.close()
+        out[fn] = {"ms_per_frame": ms / steps, "segments_per_s": segs / (ms / 1e3)}
+    mk, wf = out["rdc_render"], out["rdc_render_wavefront"]
+    return {
+        "workload": f"c2_default 1920x1080, {spp} spp per frame, 12 bounces, 81 objects",
+        "megakernel": mk, "wavefront": wf,
+        "wavefront_over_megakernel_time": wf["ms_per_frame"] / mk["ms_per_frame"],
+        "steps": steps,
+    }
+
+
 def inverse_bench(local: int, steps: int = 200, lr: float = 1e-2, spp: int = 64):
     """Config 5, inverse: recover the albedos of the 1,000 spheres nearest the
     camera in the 100k-sphere / 10k-cube scene (device LBVH) from a 512x512,
@@ -640,6 +675,10 @@ def run_ours(args):
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_bench(local, max(1, min(args.steps, 3)))
 
+    wavefront = None
+    if rank == 0 and not args.no_wavefront:
+        wavefront = wavefront_bench(local, max(1, min(args.steps, 3)))
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -688,6 +727,7 @@ def run_ours(args):
         "batched": batched,
         "large_scene": large,
         "adjoint": adjoint,
+        "wavefront_ab": wavefront,
     }
     print(json.dumps(line), flush=True)
 
@@ -704,6 +744,11 @@ def main():
         torch.cuda.set_device(_dist()[2])
         wh = [int(x) for x in args.large_only.split("x")] if args.large_only != "0" else [1920, 1080, 0]
         print(json.dumps({"large_scene": lbvh_bench(_dist()[2], max(1, min(args.steps, 2)), 0.0, *wh)}))
+        return
+    if args.wavefront_only:
+        import torch
+        torch.cuda.set_device(_dist()[2])
+        print(json.dumps({"wavefront_ab": wavefront_bench(_dist()[2], max(1, min(args.steps, 3)))}))
         return
     if args.inverse:
         import torch

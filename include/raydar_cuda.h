@@ -286,6 +286,17 @@ rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config);
  * Leaves the accumulators of the last trial; render again for results. */
 rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* best_ms_out);
 
+/* The same render as rdc_render, bit for bit, in wavefront form: per-pixel
+ * path state in device memory, one launch per bounce for the closest hits of
+ * all queued rays and one for shading them, regrouped by material class
+ * (diffuse/specular mix, metal, glass, miss) so each warp shades one class.
+ * One wave is one sample of every pixel (a CUDA graph replayed per sample),
+ * which keeps the per-pixel sample order of src/renderer/cpu.rs:198-210.
+ * Brute-force scenes only (RDC_ERR_UNSUPPORTED with an LBVH).  Provided for
+ * the megakernel / wavefront comparison; rdc_render is the faster form. */
+rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces,
+                                uint64_t seed);
+
 /* ---- differentiation (path-replay adjoint) ------------------------------
  * The reference renderer is not differentiable; these two calls add the
  * gradient of an image loss with respect to per-object material parameters,

@@ -63,6 +63,12 @@ struct rdc_ctx {
     std::vector<rdc_object> host_objects;  // copy of the uploaded scene (LBVH rebuilds)
     rdc_scene_desc host_desc{};
 
+    // wavefront render (rdc_render_wavefront)
+    char* d_wf = nullptr;
+    size_t cap_wf = 0;
+    uint32_t* d_wf_counts = nullptr;  // 6 queue lengths + the wave's sample index
+    cudaGraphExec_t wf_exec = nullptr;
+
     // differentiation (rdc_forward / rdc_backward)
     bool adj_valid = false;
     uint32_t adj_s0 = 0, adj_n = 0, adj_bounces = 0;
@@ -213,7 +219,7 @@ rdc_status apply_accel(rdc_ctx* ctx, bool scene_changed) {
     if (depth > 64) {
         ctx->bvh.release();
         ctx->bvh_active = false;
-        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the 64-entry traversal stack");
+        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the traversal stack allows (3 entries per 4-wide level)");
     }
     ctx->bvh_active = n > 0;
     ctx->bvh_depth = depth;
@@ -288,6 +294,9 @@ void rdc_destroy(rdc_ctx* ctx) {
     cudaFree(ctx->d_counters);
     cudaFree(ctx->d_grad);
     cudaFree(ctx->d_dl);
+    if (ctx->wf_exec) cudaGraphExecDestroy(ctx->wf_exec);
+    cudaFree(ctx->d_wf);
+    cudaFree(ctx->d_wf_counts);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -546,6 +555,77 @@ rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out) {
     out->kernel_launches = ctx->last_launches;
     out->h2d_bytes = ctx->h2d_bytes;
     out->d2h_bytes = ctx->d2h_bytes;
+    return RDC_OK;
+}
+
+rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces,
+                                uint64_t seed) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_render_wavefront: no scene uploaded");
+    if (max_bounces > RDC_MAX_BOUNCES)
+        return fail(ctx, RDC_ERR_LIMIT, "rdc_render_wavefront: max_bounces above RDC_MAX_BOUNCES");
+    if ((uint64_t)spp_begin + spp_count > 0xFFFFFFFFull)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_render_wavefront: sample range overflows 32 bits");
+    if (ctx->bvh_active || !ctx->brute_fits)
+        return fail(ctx, RDC_ERR_UNSUPPORTED, "rdc_render_wavefront: brute-force scenes only (no LBVH)");
+    if (rdc_status st = set_device(ctx)) return st;
+    const uint32_t npix = ctx->width * ctx->height;
+    ctx->last_paths = (uint64_t)npix * spp_count;
+    ctx->last_launches = 0;
+    ctx->last_timed = false;
+    RDC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    if (spp_count == 0) return RDC_OK;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the previous graph may still run
+    if (ctx->wf_exec) {
+        cudaGraphExecDestroy(ctx->wf_exec);
+        ctx->wf_exec = nullptr;
+    }
+    if (rdc_status st = ensure(ctx, &ctx->d_wf, &ctx->cap_wf, rdc::wavefront_state_bytes(npix), "wavefront state"))
+        return st;
+    if (!ctx->d_wf_counts) RDC_CUDA(ctx, cudaMalloc((void**)&ctx->d_wf_counts, 8 * sizeof(uint32_t)));
+    rdc::WfParams p;
+    p.sc = ctx->view;
+    p.accum = ctx->d_accum;
+    p.npix = npix;
+    p.max_bounces = max_bounces;
+    p.stream_id = 0;
+    p.key0 = (uint32_t)seed;
+    p.key1 = (uint32_t)(seed >> 32);
+    p.counts = ctx->d_wf_counts;
+    p.sample = ctx->d_wf_counts + 6;
+    p.segments = ctx->d_counters + 1;
+    float* f = reinterpret_cast<float*>(ctx->d_wf);
+    float** planes[12] = {&p.ox, &p.oy, &p.oz, &p.dx, &p.dy, &p.dz, &p.ar, &p.ag, &p.ab, &p.lr, &p.lg, &p.lb};
+    for (int i = 0; i < 12; ++i) *planes[i] = f + (size_t)i * npix;
+    p.hit_t = f + (size_t)12 * npix;
+    p.hit_obj = reinterpret_cast<int*>(f + (size_t)13 * npix);
+    uint32_t* u = reinterpret_cast<uint32_t*>(f + (size_t)14 * npix);
+    p.queue0 = u;
+    p.queue1 = u + npix;
+    p.cls = u + 2 * (size_t)npix;
+    const size_t smem = rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
+    int per_i = 0, per_s = 0;
+    RDC_CUDA(ctx, rdc::wavefront_occupancy(256, smem, &per_i, &per_s));
+    if (per_i < 1 || per_s < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_render_wavefront: kernels do not fit on an SM");
+    const int grid_i = ctx->num_sms * per_i, grid_s = ctx->num_sms * per_s;
+    RDC_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = rdc::enqueue_wave(p, grid_i, grid_s, smem, ctx->stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(ctx, e != cudaSuccess ? e : e2, "rdc_render_wavefront: capture");
+    }
+    e = cudaGraphInstantiate(&ctx->wf_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    RDC_CUDA(ctx, rdc::wavefront_set_sample(p.sample, spp_begin, ctx->stream));
+    RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    for (uint32_t k = 0; k < spp_count; ++k) RDC_CUDA(ctx, cudaGraphLaunch(ctx->wf_exec, ctx->stream));
+    RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->last_timed = true;
+    ctx->last_launches = spp_count * (2u + 2u * max_bounces);
+    ctx->sample_count = spp_begin + spp_count > ctx->sample_count ? spp_begin + spp_count : ctx->sample_count;
     return RDC_OK;
 }
 

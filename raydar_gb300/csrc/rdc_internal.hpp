@@ -115,6 +115,27 @@ size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad);
 cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, size_t smem, cudaStream_t s);
 
+// Wavefront render (rdc_wavefront.cu): per-pixel path state as planes of
+// npix floats in one buffer of wavefront_state_bytes(npix).
+struct WfParams {
+    SceneView sc;
+    float4* accum;
+    uint32_t npix, max_bounces, stream_id, key0, key1;
+    uint32_t* sample;   // the wave's sample index (device), advanced per wave
+    float *ox, *oy, *oz, *dx, *dy, *dz;  // the path's next ray
+    float *ar, *ag, *ab, *lr, *lg, *lb;  // throughput, radiance
+    float* hit_t;
+    int* hit_obj;
+    uint32_t *queue0, *queue1;  // ray queues (pixel ids), alternating per bounce
+    uint32_t* cls;              // 4 class queues of npix entries: mix, metal, glass, miss
+    uint32_t* counts;           // [0], [1] ray queue lengths, [2..5] class queue lengths
+    unsigned long long* segments;
+};
+size_t wavefront_state_bytes(uint32_t npix);
+cudaError_t wavefront_occupancy(int block, size_t smem, int* intersect_per_sm, int* shade_per_sm);
+cudaError_t wavefront_set_sample(uint32_t* sample, uint32_t v, cudaStream_t s);
+cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s);
+
 // One scene of a batch (rdc_batch_upload): its view, accumulator, sample
 // count, bounce limit, RNG key and share of the batch's estimated work.
 struct BatchScene {

@@ -1,0 +1,223 @@
+// rdc_wavefront.cu -- wavefront form of the render (sm_103a), the other side of
+// the megakernel-vs-wavefront comparison.
+//
+// The megakernel (render_kernel) keeps each path in one lane's registers from
+// its primary ray to its end.  Here a path's state lives in HBM (structure of
+// arrays indexed by pixel) and every bounce is two launches over queues:
+//   wf_intersect  one thread per queued ray: the brute-force closest hit over
+//                 the scene staged in shared memory (the megakernel's
+//                 intersect_all), then the ray's pixel is appended to one of
+//                 four class queues -- diffuse/specular mix, metal, glass,
+//                 miss -- with one warp-aggregated atomic per class;
+//   wf_shade      over the four class queues back to back, so a warp shades
+//                 one material class at a time (no divergence between the
+//                 glass, metal and rough branches of the scatter); survivors
+//                 are compacted into the next ray queue.
+// Accumulation must add a pixel's samples in sample order (the reference sums
+// sequentially, src/renderer/cpu.rs:198-210), so a wave is one sample index
+// for every pixel: generate, max_bounces x (intersect, shade), accumulate.
+// The wave is captured once as a CUDA graph and replayed per sample; the
+// sample index the RNG counter needs is read from device memory and advanced
+// by the accumulate kernel.  Results are bit-identical to render_kernel.
+#include <cstdint>
+
+#include "rdc_device.cuh"
+
+namespace rdc {
+
+namespace {
+
+__device__ __forceinline__ int material_class(const MatDev& m) {
+    if (m.c.x > 0.0f) return 2;     // transmission: the glass branch
+    if (m.b.w >= 1.0f) return 1;    // metallic 1: always the specular lobe
+    return 0;                        // the diffuse / specular draw
+}
+
+__global__ void wf_generate(const WfParams P) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        P.counts[0] = P.max_bounces > 0 ? P.npix : 0u;
+    }
+    if (i >= P.npix) return;
+    V3 o, d;
+    primary_ray(P.sc, i % P.sc.width, i / P.sc.width, o, d);
+    P.ox[i] = o.x; P.oy[i] = o.y; P.oz[i] = o.z;
+    P.dx[i] = d.x; P.dy[i] = d.y; P.dz[i] = d.z;
+    P.ar[i] = 1.0f; P.ag[i] = 1.0f; P.ab[i] = 1.0f;
+    P.lr[i] = 0.0f; P.lg[i] = 0.0f; P.lb[i] = 0.0f;
+    P.queue0[i] = i;
+}
+
+__global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint32_t* __restrict__ q_in,
+                                                     const uint32_t* __restrict__ n_in) {
+    extern __shared__ float4 smem[];
+    float4* s_rec = smem;
+    int4* s_runs = reinterpret_cast<int4*>(smem + P.sc.nrec);
+    for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
+    for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
+    __syncthreads();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = *n_in;
+    const bool scene_fast = P.sc.fast_div != 0u;
+    uint32_t segs = 0;
+    // warp-uniform trip count so the ballots below see whole warps
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t base0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    for (uint32_t wbase = base0; wbase < n; wbase += stride) {
+        const uint32_t k = wbase + lane;
+        int cls = -1;
+        uint32_t pix = 0;
+        if (k < n) {
+            pix = q_in[k];
+            const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
+            const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
+            const RayPre r = ray_pre(o, d, P.sc.neg_zero);
+            float t;
+            int idx;
+            intersect_all(s_rec, s_runs, (int)P.sc.nruns, scene_fast, r, t, idx);
+            P.hit_t[pix] = t;
+            P.hit_obj[pix] = idx;
+            ++segs;
+            cls = idx < 0 ? 3 : material_class(P.sc.mat[idx]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const unsigned m = __ballot_sync(FULL, cls == c);
+            if (m == 0u) continue;
+            const int leader = __ffs(m) - 1;
+            uint32_t b = 0;
+            if (lane == leader) b = atomicAdd(&P.counts[2 + c], (uint32_t)__popc(m));
+            b = __shfl_sync(FULL, b, leader);
+            if (cls == c) P.cls[(size_t)c * P.npix + b + __popc(m & ((1u << lane) - 1u))] = pix;
+        }
+    }
+    unsigned long long s = segs;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
+    if (lane == 0 && s != 0ull) atomicAdd(P.segments, s);
+}
+
+__global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounce, uint32_t* __restrict__ q_out,
+                                                 uint32_t* __restrict__ n_out) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t c0 = P.counts[2], c1 = P.counts[3], c2 = P.counts[4], c3 = P.counts[5];
+    const uint32_t e0 = c0, e1 = e0 + c1, e2 = e1 + c2, total = e2 + c3;
+    const uint32_t sample = *P.sample;
+    const bool more = bounce + 1u < P.max_bounces;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t base0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    for (uint32_t wbase = base0; wbase < total; wbase += stride) {
+        const uint32_t k = wbase + lane;
+        bool requeue = false;
+        uint32_t pix = 0;
+        if (k < total) {
+            const int c = k < e0 ? 0 : (k < e1 ? 1 : (k < e2 ? 2 : 3));
+            const uint32_t pos = k - (c == 0 ? 0u : (c == 1 ? e0 : (c == 2 ? e1 : e2)));
+            pix = P.cls[(size_t)c * P.npix + pos];
+            const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
+            V3 atten = mk(P.ar[pix], P.ag[pix], P.ab[pix]);
+            V3 light = mk(P.lr[pix], P.lg[pix], P.lb[pix]);
+            if (c == 3) {
+                // miss: the sky weighted by the throughput ends the path (cpu.rs:330-341)
+                const V3 sky = world_sample(P.sc, d);
+                light = vadd(light, mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z));
+            } else {
+                const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
+                const int idx = P.hit_obj[pix];
+                const MatDev m = P.sc.mat[idx];
+                const HitRec h = closest_hit(o, d, P.hit_t[pix], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
+                uint32_t w[12];
+                const uint32_t c2w = bounce * 4u;
+                const U4 w0 = philox(pix, sample, c2w, P.stream_id, P.key0, P.key1);
+                const U4 w1 = philox(pix, sample, c2w + 1u, P.stream_id, P.key0, P.key1);
+                const U4 w2 = philox(pix, sample, c2w + 2u, P.stream_id, P.key0, P.key1);
+                w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
+                w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
+                w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
+                V3 no, nd;
+                scatter(d, h, m, w, no, nd);
+                P.ox[pix] = no.x; P.oy[pix] = no.y; P.oz[pix] = no.z;
+                P.dx[pix] = nd.x; P.dy[pix] = nd.y; P.dz[pix] = nd.z;
+                atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
+                light = vadd(light, mk(m.b.x, m.b.y, m.b.z));
+                P.ar[pix] = atten.x; P.ag[pix] = atten.y; P.ab[pix] = atten.z;
+                requeue = more;
+            }
+            P.lr[pix] = light.x; P.lg[pix] = light.y; P.lb[pix] = light.z;
+        }
+        const unsigned m = __ballot_sync(FULL, requeue);
+        if (m != 0u) {
+            const int leader = __ffs(m) - 1;
+            uint32_t b = 0;
+            if (lane == leader) b = atomicAdd(n_out, (uint32_t)__popc(m));
+            b = __shfl_sync(FULL, b, leader);
+            if (requeue) q_out[b + __popc(m & ((1u << lane) - 1u))] = pix;
+        }
+    }
+}
+
+__global__ void wf_accumulate(const WfParams P) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.npix) {
+        float4 a = P.accum[i];
+        a.x = a.x + P.lr[i];
+        a.y = a.y + P.lg[i];
+        a.z = a.z + P.lb[i];
+        a.w = a.w + 1.0f;
+        P.accum[i] = a;
+    }
+    if (i == 0) *P.sample += 1u;  // nothing in this launch reads it
+}
+
+__global__ void wf_set_sample(uint32_t* sample, uint32_t v) { *sample = v; }
+
+}  // namespace
+
+size_t wavefront_state_bytes(uint32_t npix) {
+    // 12 state planes + t + obj + 2 ray queues + 4 class queues, 4 B each per pixel
+    return (size_t)npix * 4u * 20u;
+}
+
+cudaError_t wavefront_occupancy(int block, size_t smem, int* intersect_per_sm, int* shade_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(wf_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(intersect_per_sm, wf_intersect, block, smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(shade_per_sm, wf_shade, block, 0);
+    return e;
+}
+
+cudaError_t wavefront_set_sample(uint32_t* sample, uint32_t v, cudaStream_t s) {
+    wf_set_sample<<<1, 1, 0, s>>>(sample, v);
+    return cudaGetLastError();
+}
+
+// Enqueue one wave (one sample of every pixel) on s; captured into a graph by
+// the caller.  grid_i / grid_s: persistent grids of the two queue kernels.
+cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s) {
+    const uint32_t b = 256, g = (p.npix + b - 1) / b;
+    wf_generate<<<g, b, 0, s>>>(p);
+    cudaError_t e = cudaGetLastError();
+    for (uint32_t bounce = 0; bounce < p.max_bounces && e == cudaSuccess; ++bounce) {
+        uint32_t* q_in = (bounce & 1u) ? p.queue1 : p.queue0;
+        uint32_t* q_out = (bounce & 1u) ? p.queue0 : p.queue1;
+        uint32_t* n_in = p.counts + (bounce & 1u);
+        uint32_t* n_out = p.counts + ((bounce + 1u) & 1u);
+        e = cudaMemsetAsync(n_out, 0, sizeof(uint32_t), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p.counts + 2, 0, 4 * sizeof(uint32_t), s);
+        if (e != cudaSuccess) break;
+        wf_intersect<<<grid_i, 256, smem, s>>>(p, q_in, n_in);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) break;
+        wf_shade<<<grid_s, 256, 0, s>>>(p, bounce, q_out, n_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        wf_accumulate<<<g, b, 0, s>>>(p);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+}  // namespace rdc

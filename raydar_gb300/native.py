@@ -116,6 +116,7 @@ SIGNATURES = {
     "rdc_set_render_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
     "rdc_forward": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _FP]),
     "rdc_update_materials": (C.c_int, [_P, C.POINTER(RdcMaterial), C.c_uint32]),
+    "rdc_render_wavefront": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
     "rdc_backward": (C.c_int, [_P, _FP, _FP, _FP, _FP]),
     "rdc_get_render_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
     "rdc_batch_autotune": (C.c_int, [_P, C.POINTER(RdcLaunchConfig), C.POINTER(C.c_float)]),
