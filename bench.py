@@ -63,6 +63,7 @@ def _args():
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (config 4) measurement")
     p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
     p.add_argument("--no-wavefront", action="store_true", help="skip the megakernel / wavefront A/B")
+    p.add_argument("--no-refscene", action="store_true", help="skip the reference's benchmark.rscn at 3840x2160")
     p.add_argument("--wavefront-only", action="store_true", help="only the megakernel / wavefront A/B")
     p.add_argument("--inverse", action="store_true",
                    help="only the config 5 inverse-rendering run (200 Adam steps on 1000 albedos)")
@@ -461,6 +462,38 @@ def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
     }
 
 
+def reference_scene_bench(local: int, steps: int, spp: int = 16, bounces: int = 12):
+    """The reference's own benchmark scene (scenes/benchmark.rscn: 3840x2160,
+    70 spheres + 113 cubes, committed as tests/golden/benchmark.rscn), rendered
+    at full resolution, `spp` samples per frame, the default 12 bounces."""
+    from raydar_gb300 import CudaRenderer, RendererConfig
+    from raydar_gb300.roofline import ops_per_segment
+    from raydar_gb300.scene import Scene
+
+    scene = Scene.load(ROOT / "tests" / "golden" / "benchmark.rscn")
+    r = CudaRenderer(RendererConfig(max_sample_count=spp, max_bounces=bounces), device=local, seed=0)
+    r.upload(scene)
+    r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+    r.render_range(0, spp)  # warm-up
+    r.stats()
+    ms, segs = 0.0, 0
+    for k in range(steps):
+        r.seed = 300 + k
+        r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+        r.render_range(0, spp)
+        st = r.stats()
+        ms += st.device_ms
+        segs += st.segments
+    r.close()
+    n = len(scene.objects)
+    return {
+        "workload": f"scenes/benchmark.rscn: {scene.width}x{scene.height}, {n} objects (70 spheres + 113 cubes), "
+                    f"{spp} spp per frame, {bounces} bounces, brute force",
+        "segments_per_s": segs / (ms / 1e3), "kernel_ms_per_frame": ms / steps,
+        "ops_per_segment": ops_per_segment(n), "steps": steps,
+    }
+
+
 def wavefront_bench(local: int, steps: int, spp: int = 64):
     """Megakernel vs wavefront A/B on the headline scene (c2_default 1920x1080,
     12 bounces) at `spp` samples per frame: the same paths, the same
@@ -679,6 +712,10 @@ def run_ours(args):
     if rank == 0 and not args.no_wavefront:
         wavefront = wavefront_bench(local, max(1, min(args.steps, 3)))
 
+    refscene = None
+    if rank == 0 and not args.no_refscene:
+        refscene = reference_scene_bench(local, max(1, min(args.steps, 3)))
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -728,6 +765,7 @@ def run_ours(args):
         "large_scene": large,
         "adjoint": adjoint,
         "wavefront_ab": wavefront,
+        "reference_benchmark_scene": refscene,
     }
     print(json.dumps(line), flush=True)
 

@@ -153,7 +153,8 @@ rdc_status rdc_create(rdc_ctx** out, int device);
 void rdc_destroy(rdc_ctx* ctx);
 
 /* Message of the last failure on `ctx` ("" if none).  With ctx == NULL:
- * the last rdc_create failure on the calling thread. */
+ * the last failure of a call without a context (rdc_create, the .rscn
+ * reader and writer) on the calling thread. */
 const char* rdc_last_error(const rdc_ctx* ctx);
 
 /* The CUDA stream (cudaStream_t) all of the context's work is ordered on. */
@@ -163,6 +164,22 @@ rdc_status rdc_get_stream(rdc_ctx* ctx, void** stream_out);
 rdc_status rdc_synchronize(rdc_ctx* ctx);
 
 /* ---- scene ------------------------------------------------------------ */
+
+/* Read a .rscn scene -- the serde JSON the reference loads and saves
+ * (src/cli/mod.rs:32-40; layout src/scene/mod.rs:13-18, camera.rs:13-30,
+ * objects.rs:12-50, material.rs:4-13, world.rs:6-14) -- from `length` bytes of
+ * text.  The camera matrices are taken as stored.  With objects_out NULL and
+ * capacity 0 it only validates and sets *count_out; otherwise capacity must
+ * be at least the object count, and scene_out->objects = objects_out.
+ * Errors: RDC_ERR_INVALID_ARGUMENT (malformed; message in
+ * rdc_last_error(NULL)), RDC_ERR_LIMIT (capacity too small). */
+rdc_status rdc_scene_parse_rscn(const char* text, size_t length, rdc_scene_desc* scene_out,
+                                rdc_object* objects_out, uint32_t capacity, uint32_t* count_out);
+
+/* Write a scene as .rscn JSON into buf (capacity bytes, NUL-terminated);
+ * *length_out = the JSON's length without the NUL (buf NULL: length only).
+ * Floats are written with the fewest digits that read back to the same f32. */
+rdc_status rdc_scene_write_rscn(const rdc_scene_desc* scene, char* buf, size_t capacity, size_t* length_out);
 
 /* Copy a scene to the device: validates it, flattens the objects into
  * structure-of-arrays records and precomputes per-object constants.

@@ -100,7 +100,7 @@ struct rdc_ctx {
 
 namespace {
 
-thread_local std::string g_create_error;
+thread_local std::string g_create_error;  // failures without a context: rdc_last_error(NULL)
 
 rdc_status fail(rdc_ctx* ctx, rdc_status st, const std::string& msg) {
     if (ctx) ctx->err = msg;
@@ -228,6 +228,10 @@ rdc_status apply_accel(rdc_ctx* ctx, bool scene_changed) {
 }
 
 }  // namespace
+
+namespace rdc {
+void set_thread_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace rdc
 
 extern "C" {
 

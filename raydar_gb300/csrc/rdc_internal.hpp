@@ -18,6 +18,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -114,6 +115,10 @@ struct AdjParams {
 size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad);
 cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, size_t smem, cudaStream_t s);
+
+// The message rdc_last_error(NULL) returns on this thread (calls without a
+// context: rdc_create, the .rscn reader/writer).
+void set_thread_error(const std::string& msg);
 
 // Wavefront render (rdc_wavefront.cu): per-pixel path state as planes of
 // npix floats in one buffer of wavefront_state_bytes(npix).

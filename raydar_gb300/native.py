@@ -117,6 +117,9 @@ SIGNATURES = {
     "rdc_forward": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _FP]),
     "rdc_update_materials": (C.c_int, [_P, C.POINTER(RdcMaterial), C.c_uint32]),
     "rdc_render_wavefront": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
+    "rdc_scene_parse_rscn": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(RdcSceneDesc), C.POINTER(RdcObject),
+                                       C.c_uint32, C.POINTER(C.c_uint32)]),
+    "rdc_scene_write_rscn": (C.c_int, [C.POINTER(RdcSceneDesc), C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "rdc_backward": (C.c_int, [_P, _FP, _FP, _FP, _FP]),
     "rdc_get_render_config": (C.c_int, [_P, C.POINTER(RdcLaunchConfig)]),
     "rdc_batch_autotune": (C.c_int, [_P, C.POINTER(RdcLaunchConfig), C.POINTER(C.c_float)]),
