@@ -378,6 +378,10 @@ rdc_status rdc_scatter_fixed(rdc_ctx* ctx, const float* origins, const float* di
  * counterpart (it reports wall-clock timers only, src/renderer/timing.rs). */
 rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, double* sm_mhz);
 
+/* The same with packed FP32x2 FMA chains (fma.rn.f32x2), counting both
+ * components: the FP32 rate the packed two-sphere tests can reach. */
+rdc_status rdc_measure_fp32x2_issue(rdc_ctx* ctx, double* lane_ops_per_second);
+
 /* ---- host-only helpers (no GPU needed) -------------------------------- */
 
 /* Recompute a camera's view, projection and inverse matrices from its

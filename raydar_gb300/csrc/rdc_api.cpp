@@ -730,9 +730,10 @@ rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo
     return RDC_OK;
 }
 
-rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, double* sm_mhz) {
-    if (!ctx || !lane_ops_per_second) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_measure_fp32_issue: NULL argument");
-    if (rdc_status st = set_device(ctx)) return st;
+namespace {
+// Best lane-operation rate of the FFMA (packed: FP32x2 FMA, two lane
+// operations per instruction) probe over a few launches of growing length.
+rdc_status fp32_probe(rdc_ctx* ctx, bool packed, double* best_out) {
     const int block = 256, blocks_per_sm = 8;  // 64 warps per SM
     const int grid = ctx->num_sms * blocks_per_sm;
     float* sink = nullptr;
@@ -742,21 +743,38 @@ rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, dou
     cudaError_t e = cudaSuccess;
     for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {
         e = cudaEventRecord(ctx->ev0, ctx->stream);
-        if (e == cudaSuccess) e = rdc::launch_fp32_probe(sink, grid, block, iters, ctx->stream);
+        if (e == cudaSuccess) e = rdc::launch_fp32_probe(sink, grid, block, iters, packed, ctx->stream);
         if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, ctx->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
         float ms = 0.f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
         if (e != cudaSuccess) break;
-        const double ops = (double)grid * block * iters * 16.0 * rdc::kProbeChains;
+        const double ops = (double)grid * block * iters * 16.0 * rdc::kProbeChains * (packed ? 2.0 : 1.0);
         if (ms > 0.f) best = ops / (ms * 1e-3) > best ? ops / (ms * 1e-3) : best;
         if (ms < 20.f) iters *= 2;  // grow to a few tens of milliseconds
     }
     cudaFree(sink);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "rdc_measure_fp32_issue");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "FP32 probe");
+    *best_out = best;
+    ctx->last_timed = false;
+    return RDC_OK;
+}
+}  // namespace
+
+rdc_status rdc_measure_fp32x2_issue(rdc_ctx* ctx, double* lane_ops_per_second) {
+    if (!ctx || !lane_ops_per_second)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_measure_fp32x2_issue: NULL argument");
+    if (rdc_status st = set_device(ctx)) return st;
+    return fp32_probe(ctx, true, lane_ops_per_second);
+}
+
+rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, double* sm_mhz) {
+    if (!ctx || !lane_ops_per_second) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_measure_fp32_issue: NULL argument");
+    if (rdc_status st = set_device(ctx)) return st;
+    double best = 0.0;
+    if (rdc_status st = fp32_probe(ctx, false, &best)) return st;
     *lane_ops_per_second = best;
     if (sm_mhz) *sm_mhz = best / (ctx->num_sms * 128.0) / 1e6;
-    ctx->last_timed = false;
     return RDC_OK;
 }
 

@@ -446,8 +446,32 @@ __global__ void fp32_probe_kernel(float* sink, int iters) {
     if (s == -1.2345f) sink[blockIdx.x] = s;
 }
 
-cudaError_t launch_fp32_probe(float* sink, int grid, int block, int iters, cudaStream_t s) {
-    fp32_probe_kernel<<<grid, block, 0, s>>>(sink, iters);
+// The same with packed FP32x2 FMAs (fma.rn.f32x2): two lane operations per
+// instruction, so the two probes together show whether the packed form
+// raises the FP32 rate or only saves issue slots.
+__global__ void fp32x2_probe_kernel(float* sink, int iters) {
+    float2 a[kProbeChains];
+#pragma unroll
+    for (int j = 0; j < kProbeChains; ++j) a[j] = make_float2(__int2float_rn(threadIdx.x + j), __int2float_rn(j));
+    const float2 m = make_float2(0.999999f, 0.999998f), c = make_float2(1e-7f, 2e-7f);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+#pragma unroll
+            for (int j = 0; j < kProbeChains; ++j) a[j] = fma2(a[j], m, c);
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < kProbeChains; ++j) s += a[j].x + a[j].y;
+    if (s == -1.2345f) sink[blockIdx.x] = s;
+}
+
+cudaError_t launch_fp32_probe(float* sink, int grid, int block, int iters, bool packed, cudaStream_t s) {
+    if (packed)
+        fp32x2_probe_kernel<<<grid, block, 0, s>>>(sink, iters);
+    else
+        fp32_probe_kernel<<<grid, block, 0, s>>>(sink, iters);
     return cudaGetLastError();
 }
 

@@ -131,6 +131,7 @@ SIGNATURES = {
     "rdc_scatter_fixed": (C.c_int, [_P, _FP, _FP, _FP, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
                                     C.c_uint32, _FP, _FP]),
     "rdc_measure_fp32_issue": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "rdc_measure_fp32x2_issue": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "rdc_camera_update_matrices": (C.c_int, [C.POINTER(RdcCamera)]),
 }
 
