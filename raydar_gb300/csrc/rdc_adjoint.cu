@@ -190,13 +190,14 @@ __global__ void __launch_bounds__(kRenderBlock, 2) adjoint_kernel(const AdjParam
     float4* s_rec = smem;
     int4* s_runs = reinterpret_cast<int4*>(smem + (kBvh ? 0u : P.sc.nrec));
     float* s_grad = reinterpret_cast<float*>(s_runs + (kBvh ? 0u : P.sc.nruns));
-    if (!kBvh) {
-        for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
-        for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
-    }
+    __shared__ __align__(8) uint64_t s_bar;
     if (P.smem_grad)
         for (uint32_t i = threadIdx.x; i < 8u * P.sc.nobj; i += blockDim.x) s_grad[i] = 0.0f;
+    if (!kBvh && threadIdx.x == 0) bulk_init(&s_bar);
     __syncthreads();
+    if (!kBvh &&
+        !stage_scene(&s_bar, 0u, s_rec, P.sc.rec, P.sc.nrec, s_runs, P.sc.runs, P.sc.nruns, P.errors))
+        return;
     float* gbase = P.smem_grad ? s_grad : P.grad;
     const bool scene_fast = P.sc.fast_div != 0u;
     BruteIsect brute{s_rec, s_runs, (int)P.sc.nruns, scene_fast};

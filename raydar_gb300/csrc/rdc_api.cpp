@@ -20,6 +20,8 @@ using rdc::MatDev;
 
 // Shared memory a block may use for the staged scene (records + runs).
 constexpr size_t kMaxSceneSmem = 200 * 1024;
+constexpr size_t kCounters = 8;       // device counters per context
+constexpr size_t kErrorCounter = 4;   // index of the device-error count
 
 struct rdc_ctx {
     int device = 0;
@@ -44,7 +46,9 @@ struct rdc_ctx {
     uchar4* d_rgba = nullptr;
     size_t cap_rgba = 0;
 
-    // counters: [0] work counter (u32 in the low word), [1] segments
+    // counters: [0] work counter (u32 in the low word), [1] segments, [2] node
+    // visits, [3] object tests (cleared per launch), [4] device errors (sticky
+    // until reported)
     unsigned long long* d_counters = nullptr;
 
     // last render
@@ -135,6 +139,19 @@ rdc_status ensure(rdc_ctx* ctx, T** ptr, size_t* cap, size_t n, const char* what
 rdc_status set_device(rdc_ctx* ctx) {
     RDC_CUDA(ctx, cudaSetDevice(ctx->device));
     return RDC_OK;
+}
+
+// Kernels count blocks that could not stage the scene into shared memory
+// (a bulk copy whose completion they stopped waiting for, rdc_device.cuh);
+// after a synchronisation the count is reported once as RDC_ERR_DEVICE.
+rdc_status check_device_errors(rdc_ctx* ctx) {
+    unsigned long long n = 0;
+    RDC_CUDA(ctx, cudaMemcpy(&n, ctx->d_counters + kErrorCounter, sizeof(n), cudaMemcpyDeviceToHost));
+    if (n == 0) return RDC_OK;
+    RDC_CUDA(ctx, cudaMemset(ctx->d_counters + kErrorCounter, 0, sizeof(n)));
+    return fail(ctx, RDC_ERR_DEVICE,
+                std::to_string(n) + " block(s) could not stage the scene into shared memory (bulk copy did not "
+                                    "complete); their pixels were not rendered");
 }
 
 // Checks shared by every scene entry point.  The reference accepts any
@@ -275,9 +292,9 @@ rdc_status rdc_create(rdc_ctx** out, int device) {
         return bail(e, "cudaStreamCreate");
     if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
-    if ((e = cudaMalloc((void**)&ctx->d_counters, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = cudaMalloc((void**)&ctx->d_counters, kCounters * sizeof(unsigned long long))) != cudaSuccess)
         return bail(e, "cudaMalloc(counters)");
-    if ((e = cudaMemset(ctx->d_counters, 0, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = cudaMemset(ctx->d_counters, 0, kCounters * sizeof(unsigned long long))) != cudaSuccess)
         return bail(e, "cudaMemset(counters)");
     *out = ctx;
     return RDC_OK;
@@ -322,7 +339,7 @@ rdc_status rdc_synchronize(rdc_ctx* ctx) {
     if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
     if (rdc_status st = set_device(ctx)) return st;
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return RDC_OK;
+    return check_device_errors(ctx);
 }
 
 rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
@@ -463,6 +480,7 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
     p.npix = ctx->width * ctx->height;
     p.work_counter = reinterpret_cast<uint32_t*>(ctx->d_counters);
     p.segments = ctx->d_counters + 1;
+    p.errors = ctx->d_counters + kErrorCounter;
 
     if (!ctx->bvh_active && !ctx->brute_fits)
         return fail(ctx, RDC_ERR_LIMIT,
@@ -508,7 +526,7 @@ rdc_status rdc_read_accum(rdc_ctx* ctx, float* rgba_out, size_t count) {
                                   ctx->stream));
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->d2h_bytes += need * sizeof(float);
-    return RDC_OK;
+    return check_device_errors(ctx);
 }
 
 rdc_status rdc_write_accum(rdc_ctx* ctx, const float* rgba_in, size_t count, uint32_t sample_count) {
@@ -538,13 +556,14 @@ rdc_status rdc_read_rgba8(rdc_ctx* ctx, uint32_t sample_count, uint8_t* rgba_out
     RDC_CUDA(ctx, cudaMemcpyAsync(rgba_out, ctx->d_rgba, npix * 4, cudaMemcpyDeviceToHost, ctx->stream));
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->d2h_bytes += npix * 4;
-    return RDC_OK;
+    return check_device_errors(ctx);
 }
 
 rdc_status rdc_stats_get(rdc_ctx* ctx, rdc_stats* out) {
     if (!ctx || !out) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_stats_get: NULL argument");
     if (rdc_status st = set_device(ctx)) return st;
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (rdc_status st = check_device_errors(ctx)) return st;
     unsigned long long c[4] = {0, 0, 0, 0};
     RDC_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
     out->segments = c[1];
@@ -598,6 +617,7 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     p.counts = ctx->d_wf_counts;
     p.sample = ctx->d_wf_counts + 6;
     p.segments = ctx->d_counters + 1;
+    p.errors = ctx->d_counters + kErrorCounter;
     float* f = reinterpret_cast<float*>(ctx->d_wf);
     float** planes[12] = {&p.ox, &p.oy, &p.oz, &p.dx, &p.dy, &p.dz, &p.ar, &p.ag, &p.ab, &p.lr, &p.lg, &p.lb};
     for (int i = 0; i < 12; ++i) *planes[i] = f + (size_t)i * npix;
@@ -692,6 +712,7 @@ rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo
         p.key1 = (uint32_t)(ctx->adj_seed >> 32);
         p.npaths = (uint64_t)npix * ctx->adj_n;
         p.segments = ctx->d_counters + 1;
+        p.errors = ctx->d_counters + kErrorCounter;
         const bool bvh = ctx->bvh_active;
         if (!bvh && !ctx->brute_fits)
             return fail(ctx, RDC_ERR_LIMIT, "rdc_backward: brute force needs the records in shared memory");
@@ -887,6 +908,7 @@ rdc_status capture_batch_graph(rdc_ctx* ctx) {
     p.refill_min = b.cfg.refill_min_idle;
     p.pixel_counters = b.d_pixel_counters;
     p.segments = ctx->d_counters + 1;
+    p.errors = ctx->d_counters + kErrorCounter;
     RDC_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemsetAsync(b.d_accum, 0, b.accum_total * sizeof(float4), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.d_pixel_counters, 0, b.n * sizeof(uint32_t), ctx->stream);

@@ -507,6 +507,75 @@ __device__ __forceinline__ void primary_ray(const SceneView& sc, uint32_t x, uin
 }
 
 // --------------------------------------------------------------- a path ---
+// Scene staging into shared memory with the Tensor Memory Accelerator's bulk
+// copy (cp.async.bulk, global -> shared), completing on an mbarrier.  One
+// thread initialises the barrier (bulk_init) and issues the copies
+// (bulk_issue); every thread of the block waits for the barrier's phase
+// (bulk_wait), polling at most kBulkWaitPolls times so that a copy that never
+// lands cannot hang the block: the kernel then records a device error and
+// returns.  Sources and destinations are 16-byte aligned and the sizes are
+// 16-byte multiples (float4 / int4 records).
+constexpr uint32_t kBulkWaitPolls = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void bulk_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_issue(uint64_t* bar, void* s0, const void* g0, uint32_t n0, void* s1,
+                                           const void* g1, uint32_t n1) {
+    const uint32_t b = smem_addr(bar);
+    // order the block's earlier generic reads of this shared memory before the async writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(b),
+                 "r"(n0 + n1)
+                 : "memory");
+    if (n0)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_addr(s0)),
+                     "l"(g0), "r"(n0), "r"(b)
+                     : "memory");
+    if (n1)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_addr(s1)),
+                     "l"(g1), "r"(n1), "r"(b)
+                     : "memory");
+}
+
+// true once the barrier's phase `parity` has completed (bounded polling).
+__device__ __forceinline__ bool bulk_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t b = smem_addr(bar);
+    for (uint32_t i = 0; i < kBulkWaitPolls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(b), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Stage a scene's records and runs (brute-force kernels): thread 0 issues,
+// all wait.  Returns false for the whole block if the copy did not land
+// (then errors[0] is incremented once and the block must return).
+__device__ __forceinline__ bool stage_scene(uint64_t* bar, uint32_t parity, float4* s_rec, const float4* rec,
+                                            uint32_t nrec, int4* s_runs, const int4* runs, uint32_t nruns,
+                                            unsigned long long* errors) {
+    if (threadIdx.x == 0) bulk_issue(bar, s_rec, rec, 16u * nrec, s_runs, runs, 16u * nruns);
+    const bool ok = __syncthreads_and(bulk_wait(bar, parity)) != 0;
+    if (!ok && threadIdx.x == 0) {
+        if (errors) atomicAdd(errors, 1ull);
+        bulk_wait(bar, parity);  // give copies still in flight a last bounded chance to land
+    }
+    return ok;
+}
+
 struct PathState {
     V3 o, d, atten, light;
     uint32_t bounce;

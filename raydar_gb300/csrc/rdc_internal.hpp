@@ -97,6 +97,7 @@ struct RenderParams {
     uint32_t* work_counter;
     unsigned long long* segments;
     uint32_t min_idle;                // render_bvh_kernel: lanes done before a warp shades
+    unsigned long long* errors;       // device errors (shared-memory staging that did not complete)
 };
 
 // Path-replay adjoint (rdc_adjoint.cu).  grad holds 8 floats per object:
@@ -111,6 +112,7 @@ struct AdjParams {
     uint64_t npaths;    // npix * nspp
     unsigned long long* segments;
     uint32_t smem_grad; // 1: per-block shared accumulators (8 * nobj floats)
+    unsigned long long* errors;  // device errors (shared-memory staging that did not complete)
 };
 size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad);
 cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm);
@@ -135,6 +137,7 @@ struct WfParams {
     uint32_t* cls;              // 4 class queues of npix entries: mix, metal, glass, miss
     uint32_t* counts;           // [0], [1] ray queue lengths, [2..5] class queue lengths
     unsigned long long* segments;
+    unsigned long long* errors;  // device errors (shared-memory staging that did not complete)
 };
 size_t wavefront_state_bytes(uint32_t npix);
 cudaError_t wavefront_occupancy(int block, size_t smem, int* intersect_per_sm, int* shade_per_sm);
@@ -160,6 +163,7 @@ struct BatchParams {
     uint32_t refill_min;      // idle lanes of a warp that trigger a refill (regroup period)
     uint32_t* pixel_counters; // per scene: next pixel to hand out
     unsigned long long* segments;
+    unsigned long long* errors;  // device errors (shared-memory staging that did not complete)
 };
 
 // Kernel launchers (rdc_kernels.cu).  Each returns the cudaError_t of its

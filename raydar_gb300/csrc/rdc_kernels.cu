@@ -86,11 +86,12 @@ __device__ __forceinline__ void add_warp_sum(unsigned long long* dst, unsigned l
 // Brute force: the scene's records are staged in shared memory per block.
 __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderParams P) {
     extern __shared__ float4 smem[];
+    __shared__ __align__(8) uint64_t s_bar;
     float4* s_rec = smem;
     int4* s_runs = reinterpret_cast<int4*>(smem + P.sc.nrec);
-    for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
-    for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
+    if (threadIdx.x == 0) bulk_init(&s_bar);
     __syncthreads();
+    if (!stage_scene(&s_bar, 0u, s_rec, P.sc.rec, P.sc.nrec, s_runs, P.sc.runs, P.sc.nruns, P.errors)) return;
     BruteIsect isect{s_rec, s_runs, (int)P.sc.nruns, P.sc.fast_div != 0u};
     const uint32_t segs = render_loop(P, isect);
     add_warp_sum(P.segments, segs);
@@ -270,14 +271,17 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
     extern __shared__ float4 smem[];
     __shared__ BatchScene s_bs;
     __shared__ int s_scene;
+    __shared__ __align__(8) uint64_t s_bar;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < 32) {
         const int sc0 = batch_initial_scene(P, ((float)blockIdx.x + 0.5f) / (float)gridDim.x, lane);
         if (lane == 0) s_scene = sc0;
     }
+    if (threadIdx.x == 0) bulk_init(&s_bar);
     __syncthreads();
     uint32_t segs = 0;
+    uint32_t phase = 0;  // of s_bar: one completed phase per staged scene
 
     for (;;) {
         const int scene = s_scene;
@@ -291,9 +295,10 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
         __syncthreads();
         float4* s_rec = smem;
         int4* s_runs = reinterpret_cast<int4*>(smem + s_bs.sc.nrec);
-        for (uint32_t i = threadIdx.x; i < s_bs.sc.nrec; i += blockDim.x) s_rec[i] = s_bs.sc.rec[i];
-        for (uint32_t i = threadIdx.x; i < s_bs.sc.nruns; i += blockDim.x) s_runs[i] = s_bs.sc.runs[i];
-        __syncthreads();
+        if (!stage_scene(&s_bar, phase, s_rec, s_bs.sc.rec, s_bs.sc.nrec, s_runs, s_bs.sc.runs, s_bs.sc.nruns,
+                         P.errors))
+            return;
+        phase ^= 1u;
 
         const uint32_t npix = s_bs.npix;
         uint32_t* counter = P.pixel_counters + scene;

@@ -176,8 +176,8 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
             e = cudaMemcpyAsync(d_runs, g_stage_runs, fc.nruns * sizeof(int4), cudaMemcpyHostToDevice, s);
     }
     if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemcpyAsync(scene)");
-    // The work counter and the segment counter must start at zero.
-    e = cudaMemsetAsync(d_counters, 0, 2 * sizeof(unsigned long long), s);
+    // The work counter, the segment counter and the device-error count start at zero.
+    e = cudaMemsetAsync(d_counters, 0, 5 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemsetAsync(counters)");
 
     if (spp_count > 0) {
@@ -215,6 +215,7 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
         p.npix = cam.resolution_x * cam.resolution_y;
         p.work_counter = reinterpret_cast<uint32_t*>(d_counters);
         p.segments = d_counters + 1;
+        p.errors = d_counters + 4;
         p.min_idle = 1;
 
         const size_t smem = rdc::render_smem_bytes(fc.nrec, fc.nruns);
@@ -233,11 +234,16 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
         if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "render launch");
     }
     if (segments_out) {
-        unsigned long long segs = 0;
-        e = cudaMemcpyAsync(&segs, d_counters + 1, sizeof(segs), cudaMemcpyDeviceToHost, s);
+        unsigned long long c[5] = {0, 0, 0, 0, 0};
+        e = cudaMemcpyAsync(c, d_counters, sizeof(c), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "segment read-back");
-        *segments_out = segs;
+        *segments_out = c[1];
+        if (c[4] != 0) {
+            set_error(error_out, error_capacity,
+                      "rdc_render_static: a block could not stage the scene into shared memory");
+            return RDC_ERR_DEVICE;
+        }
     }
     return RDC_OK;
 }

@@ -51,11 +51,12 @@ __global__ void wf_generate(const WfParams P) {
 __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint32_t* __restrict__ q_in,
                                                      const uint32_t* __restrict__ n_in) {
     extern __shared__ float4 smem[];
+    __shared__ __align__(8) uint64_t s_bar;
     float4* s_rec = smem;
     int4* s_runs = reinterpret_cast<int4*>(smem + P.sc.nrec);
-    for (uint32_t i = threadIdx.x; i < P.sc.nrec; i += blockDim.x) s_rec[i] = P.sc.rec[i];
-    for (uint32_t i = threadIdx.x; i < P.sc.nruns; i += blockDim.x) s_runs[i] = P.sc.runs[i];
+    if (threadIdx.x == 0) bulk_init(&s_bar);
     __syncthreads();
+    if (!stage_scene(&s_bar, 0u, s_rec, P.sc.rec, P.sc.nrec, s_runs, P.sc.runs, P.sc.nruns, P.errors)) return;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t n = *n_in;
