@@ -382,6 +382,12 @@ rdc_status rdc_measure_fp32_issue(rdc_ctx* ctx, double* lane_ops_per_second, dou
  * components: the FP32 rate the packed two-sphere tests can reach. */
 rdc_status rdc_measure_fp32x2_issue(rdc_ctx* ctx, double* lane_ops_per_second);
 
+/* Self-test of the device-error path: runs one block whose shared-memory
+ * staging wait cannot complete (the barrier expects bytes no copy delivers),
+ * so the wait gives up after its bounded polls.  Returns RDC_ERR_DEVICE with
+ * the message a render would give; the context stays usable. */
+rdc_status rdc_selftest_staging_timeout(rdc_ctx* ctx);
+
 /* ---- host-only helpers (no GPU needed) -------------------------------- */
 
 /* Recompute a camera's view, projection and inverse matrices from its

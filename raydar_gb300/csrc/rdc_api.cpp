@@ -782,6 +782,16 @@ rdc_status fp32_probe(rdc_ctx* ctx, bool packed, double* best_out) {
 }
 }  // namespace
 
+rdc_status rdc_selftest_staging_timeout(rdc_ctx* ctx) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (rdc_status st = set_device(ctx)) return st;
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (rdc_status st = check_device_errors(ctx)) return st;  // report anything earlier first
+    RDC_CUDA(ctx, rdc::launch_staging_timeout(ctx->d_counters + kErrorCounter, ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_device_errors(ctx);
+}
+
 rdc_status rdc_measure_fp32x2_issue(rdc_ctx* ctx, double* lane_ops_per_second) {
     if (!ctx || !lane_ops_per_second)
         return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_measure_fp32x2_issue: NULL argument");

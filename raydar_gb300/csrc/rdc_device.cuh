@@ -546,15 +546,20 @@ __device__ __forceinline__ void bulk_issue(uint64_t* bar, void* s0, const void* 
                      : "memory");
 }
 
-// true once the barrier's phase `parity` has completed (bounded polling).
+// true once the barrier's phase `parity` has completed.  Each poll suspends
+// the thread for at most kBulkPollNs (the instruction's suspend-time hint), so
+// the whole wait is bounded by about kBulkWaitPolls * kBulkPollNs (~1 s).
+constexpr uint32_t kBulkPollNs = 1000;
+
 __device__ __forceinline__ bool bulk_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t b = smem_addr(bar);
     for (uint32_t i = 0; i < kBulkWaitPolls; ++i) {
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(b), "r"(parity)
+            : "r"(b), "r"(parity), "r"(kBulkPollNs)
             : "memory");
         if (done) return true;
     }

@@ -185,6 +185,7 @@ cudaError_t launch_scatter_fixed(const SceneView& sc, const float* o, const floa
                                  uint32_t n, float* o_out, float* d_out, cudaStream_t s);
 
 cudaError_t launch_fp32_probe(float* sink, int grid, int block, int iters, bool packed, cudaStream_t s);
+cudaError_t launch_staging_timeout(unsigned long long* errors, cudaStream_t s);
 
 // A cube whose slab bounds keep the kernels' exact reciprocal division in
 // range (rdc_device.cuh): positive finite side, every bound 0 or with

@@ -451,6 +451,28 @@ __global__ void fp32_probe_kernel(float* sink, int iters) {
     if (s == -1.2345f) sink[blockIdx.x] = s;
 }
 
+// Self-test of the staging wait's limit: the barrier expects 16 bytes that
+// no copy will deliver (nothing is issued), so bulk_wait gives up after its
+// bounded polls and the block records a device error and returns, exactly as
+// a render block whose copy did not land.  Nothing is in flight at any time.
+__global__ void staging_timeout_kernel(unsigned long long* errors) {
+    __shared__ __align__(8) uint64_t s_bar;
+    if (threadIdx.x == 0) {
+        bulk_init(&s_bar);
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], 16;\n\t}" ::"r"(
+                         smem_addr(&s_bar))
+                     : "memory");
+    }
+    __syncthreads();
+    const bool ok = __syncthreads_and(bulk_wait(&s_bar, 0u)) != 0;
+    if (!ok && threadIdx.x == 0) atomicAdd(errors, 1ull);
+}
+
+cudaError_t launch_staging_timeout(unsigned long long* errors, cudaStream_t s) {
+    staging_timeout_kernel<<<1, 32, 0, s>>>(errors);
+    return cudaGetLastError();
+}
+
 // The same with packed FP32x2 FMAs (fma.rn.f32x2): two lane operations per
 // instruction, so the two probes together show whether the packed form
 // raises the FP32 rate or only saves issue slots.

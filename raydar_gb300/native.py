@@ -132,6 +132,7 @@ SIGNATURES = {
                                     C.c_uint32, _FP, _FP]),
     "rdc_measure_fp32_issue": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "rdc_measure_fp32x2_issue": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "rdc_selftest_staging_timeout": (C.c_int, [_P]),
     "rdc_camera_update_matrices": (C.c_int, [C.POINTER(RdcCamera)]),
 }
 

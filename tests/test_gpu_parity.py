@@ -291,3 +291,16 @@ def test_device_min_max_signed_zero_semantics(renderer):
                                            native.iptr(idx), native.fptr(nrm), native.u8ptr(fr)) == 0
     rt, ridx, rn, rf = oracle.intersect(scene.to_c(), o, d)
     assert np.array_equal(idx, ridx) and bits_equal(t, rt) and bits_equal(nrm, rn)
+
+
+def test_staging_wait_limit_reports_a_device_error_and_the_context_survives(renderer):
+    """The shared-memory staging wait gives up after its bounded polls (here on
+    a barrier nothing completes): RDC_ERR_DEVICE comes back once, then the
+    context renders bit-identically to the oracle again."""
+    st = renderer.lib.rdc_selftest_staging_timeout(renderer.ctx)
+    assert st == 7, st  # RDC_ERR_DEVICE
+    assert b"shared memory" in renderer.lib.rdc_last_error(renderer.ctx)
+    scene = SCENES["c1_64x36"]()
+    acc, seg = _render_gpu(renderer, scene, 0, 2, 8, seed=77)
+    ref, ref_seg = oracle.render(scene.to_c(), 0, 2, 8, 77, threads=8)
+    assert seg == ref_seg and bits_equal(acc, ref)
