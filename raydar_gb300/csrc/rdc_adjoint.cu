@@ -45,7 +45,7 @@ struct AdjVert {
 // Reverse step through vertex v: (go, gd) are the adjoints of the ray that
 // leaves v; returns those of the ray that reaches v and dL/d(roughness^2).
 __device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& v, V3& go, V3& gd) {
-    const MatDev m = sc.mat[v.obj];
+    const MatDev m = load_mat(sc.mat, v.obj);
     const float4 hi = __ldg(&sc.hit[v.obj]);
     const int kind = __float_as_int(m.d.y);
     const HitRec h = closest_hit(v.o, v.d, v.t, hi, kind);
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) adjoint_kernel(const AdjParam
                         missed = true;
                         break;
                     }
-                    const MatDev m = P.sc.mat[idx];
+                    const MatDev m = load_mat(P.sc.mat, idx);
                     const HitRec h = closest_hit(o, d, t, __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
                     uint32_t w[12];
                     const uint32_t c2 = b * 4u;

@@ -87,8 +87,8 @@ __device__ __forceinline__ void bvh_sphere_leaf(const RayPre& r, float4 p0, floa
 
 template <bool Fast>
 __device__ __forceinline__ void bvh_leaf(const BvhView& bv, const RayPre& r, int obj, float& best, int& bidx) {
-    const float4 p0 = __ldg(&bv.prims[2 * obj]);
-    const float4 p1 = __ldg(&bv.prims[2 * obj + 1]);
+    float4 p0, p1;
+    ldg_pair(bv.prims + 2 * obj, p0, p1);
     if (__float_as_int(p1.w) == RDC_GEOMETRY_SPHERE) {
         bvh_sphere_leaf<Fast>(r, p0, p1.x, obj, best, bidx);
     } else {
@@ -197,10 +197,7 @@ __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, boo
     const float4* np = bv.nodes[T.cur].v;
     float4 lo[4], hi[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        lo[j] = __ldg(np + 2 * j);
-        hi[j] = __ldg(np + 2 * j + 1);
-    }
+    for (int j = 0; j < 4; ++j) ldg_pair(np + 2 * j, lo[j], hi[j]);
     ++cnt.visits;
     // limit: skip a box whose entry exceeds best (relative slack for the box test's rounding)
     const float limit = T.best * 1.0000038f + 1e-30f;

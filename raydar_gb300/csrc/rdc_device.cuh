@@ -98,6 +98,16 @@ __device__ __forceinline__ float div_recip(float a, float b, float y) {
     return __fmaf_rn(r, y, q0);
 }
 
+// A 32-byte record (two float4, 32-byte aligned) with one 256-bit read-only
+// load: half the load instructions and L1 wavefronts of two 128-bit loads
+// when the lanes of a warp read different records (BVH nodes, primitives,
+// materials).
+__device__ __forceinline__ void ldg_pair(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 __device__ __forceinline__ bool in_range(float v, float lo, float hi) {
     const float m = fabsf(v);
     return m >= lo && m <= hi;
@@ -345,6 +355,15 @@ struct HitRec {
     V3 p, n;
     bool front;
 };
+
+// An object's material record (64 bytes, 64-byte aligned): two 256-bit loads.
+__device__ __forceinline__ MatDev load_mat(const MatDev* mats, int i) {
+    MatDev m;
+    const float4* p = reinterpret_cast<const float4*>(mats + i);
+    ldg_pair(p, m.a, m.b);
+    ldg_pair(p + 2, m.c, m.d);
+    return m;
+}
 
 // closest_hit, src/renderer/cpu.rs:354-394.
 __device__ __forceinline__ HitRec closest_hit(V3 o, V3 d, float t, float4 hi, int kind) {
@@ -620,7 +639,7 @@ __device__ __forceinline__ bool segment_shade(const SceneView& sc, PathState& s,
         return true;
     }
     const float4 hi = __ldg(&sc.hit[idx]);
-    const MatDev m = sc.mat[idx];
+    const MatDev m = load_mat(sc.mat, idx);
     const HitRec h = closest_hit(s.o, s.d, t, hi, __float_as_int(m.d.y));
     uint32_t w[12];
     const uint32_t c2 = s.bounce * 4u;

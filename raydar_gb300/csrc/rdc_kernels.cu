@@ -388,7 +388,7 @@ __global__ void intersect_rays_kernel(const SceneView sc, const BvhView bvh, con
     }
     idx_out[i] = idx;
     if (idx >= 0) {
-        const MatDev m = sc.mat[idx];
+        const MatDev m = load_mat(sc.mat, idx);
         const HitRec h = closest_hit(ro, rd, t, sc.hit[idx], __float_as_int(m.d.y));
         t_out[i] = t;
         n_out[3 * i] = h.n.x;
@@ -415,7 +415,7 @@ __global__ void scatter_fixed_kernel(const SceneView sc, const float* __restrict
     if (k < 0 || (uint32_t)k >= sc.nobj) return;  // rejected on the host; never reached
     const V3 ro = mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
     const V3 rd = mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
-    const MatDev m = sc.mat[k];
+    const MatDev m = load_mat(sc.mat, k);
     const HitRec h = closest_hit(ro, rd, t[i], sc.hit[k], __float_as_int(m.d.y));
     uint32_t w[12];
 #pragma unroll

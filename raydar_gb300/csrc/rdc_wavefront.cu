@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
             } else {
                 const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
                 const int idx = P.hit_obj[pix];
-                const MatDev m = P.sc.mat[idx];
+                const MatDev m = load_mat(P.sc.mat, idx);
                 const HitRec h = closest_hit(o, d, P.hit_t[pix], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
                 uint32_t w[12];
                 const uint32_t c2w = bounce * 4u;
