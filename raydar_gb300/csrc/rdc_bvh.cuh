@@ -192,8 +192,8 @@ __device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb
 // internal child hit is visited next and the others pushed, farthest first;
 // with none, the next stacked box still in front of the best hit, or none
 // (T.cur = -1).
-__device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T,
-                                         int* stack_node, float* stack_entry, BvhCounters& cnt) {
+__device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T, uint2* stack,
+                                         BvhCounters& cnt) {
     const float4* np = bv.nodes[T.cur].v;
     float4 lo[4], hi[4];
 #pragma unroll
@@ -226,29 +226,18 @@ __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, boo
     bvh_cswap(k1, v1, k3, v3);
     bvh_cswap(k1, v1, k2, v2);
     if (k0 != INF) {
-        if (k3 != INF) {
-            stack_node[T.sp] = v3;
-            stack_entry[T.sp] = k3;
-            ++T.sp;
-        }
-        if (k2 != INF) {
-            stack_node[T.sp] = v2;
-            stack_entry[T.sp] = k2;
-            ++T.sp;
-        }
-        if (k1 != INF) {
-            stack_node[T.sp] = v1;
-            stack_entry[T.sp] = k1;
-            ++T.sp;
-        }
+        // an entry is (node, entry distance bits): one 8-byte local store or load
+        if (k3 != INF) stack[T.sp++] = make_uint2((unsigned)v3, __float_as_uint(k3));
+        if (k2 != INF) stack[T.sp++] = make_uint2((unsigned)v2, __float_as_uint(k2));
+        if (k1 != INF) stack[T.sp++] = make_uint2((unsigned)v1, __float_as_uint(k1));
         T.cur = v0;
     } else {
         // pop the next box still in front of the best hit
         int next = -1;
         while (T.sp > 0) {
-            --T.sp;
-            if (stack_entry[T.sp] <= lim) {
-                next = stack_node[T.sp];
+            const uint2 top = stack[--T.sp];
+            if (__uint_as_float(top.y) <= lim) {
+                next = (int)top.x;
                 break;
             }
         }
@@ -269,15 +258,14 @@ __device__ __forceinline__ void bvh_leaf_step(const BvhView& bv, const RayPre& r
 // Closest hit through the BVH: the same (t, index) the brute-force loop gives.
 __device__ __forceinline__ void bvh_intersect(const BvhView& bv, const RayPre& r, bool fast, float& best, int& bidx,
                                               BvhCounters& cnt) {
-    int stack_node[kBvhStack];
-    float stack_entry[kBvhStack];
+    uint2 stack[kBvhStack];
     BvhTrav T;
     bvh_begin(bv, r, fast, T, cnt);
     while (T.cur >= 0 || T.lmask != 0u) {
         if (T.lmask != 0u)
             bvh_leaf_step(bv, r, fast, T, cnt);
         else
-            bvh_step(bv, r, fast, T, stack_node, stack_entry, cnt);
+            bvh_step(bv, r, fast, T, stack, cnt);
     }
     best = T.best;
     bidx = T.bidx;

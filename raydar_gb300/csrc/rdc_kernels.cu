@@ -119,8 +119,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const bool scene_fast = P.sc.fast_div != 0u;
-    int stack_node[kBvhStack];
-    float stack_entry[kBvhStack];
+    uint2 stack[kBvhStack];
     BvhCounters cnt;
     BvhTrav T;
     T.cur = -1;
@@ -215,7 +214,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
             if (__popc(lm) >= __popc(nm)) {
                 if (wl) bvh_leaf_step(P.bvh, r, rfast, T, cnt);
             } else {
-                if (wn) bvh_step(P.bvh, r, rfast, T, stack_node, stack_entry, cnt);
+                if (wn) bvh_step(P.bvh, r, rfast, T, stack, cnt);
             }
         }
     }
