@@ -175,6 +175,37 @@ __device__ __forceinline__ void bvh_begin(const BvhView& bv, const RayPre& r, bo
     T.cur = 0;
 }
 
+// Traversal stacks of (node, entry distance bits) words.  LocalStack: one
+// per-thread local array.  SplitStack: the first kShortStack entries in
+// shared memory (entry k of thread t at sh[k * stride], sh already offset by
+// t; consecutive threads, consecutive words, no bank conflicts), deeper ones
+// in the local array; shared memory needs no tag lookup and leaves the L1 to
+// the nodes.
+constexpr int kShortStack = 16;
+
+struct LocalStack {
+    uint2* a;
+    __device__ __forceinline__ void push(int& sp, uint2 e) { a[sp++] = e; }
+    __device__ __forceinline__ uint2 pop(int& sp) { return a[--sp]; }
+};
+
+struct SplitStack {
+    uint2* sh;
+    uint32_t stride;
+    uint2* loc;
+    __device__ __forceinline__ void push(int& sp, uint2 e) {
+        if (sp < kShortStack)
+            sh[(uint32_t)sp * stride] = e;
+        else
+            loc[sp - kShortStack] = e;
+        ++sp;
+    }
+    __device__ __forceinline__ uint2 pop(int& sp) {
+        --sp;
+        return sp < kShortStack ? sh[(uint32_t)sp * stride] : loc[sp - kShortStack];
+    }
+};
+
 // Compare-exchange of (entry, node) pairs, ascending by entry.
 __device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb) {
     const bool sw = kb < ka;
@@ -192,7 +223,8 @@ __device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb
 // internal child hit is visited next and the others pushed, farthest first;
 // with none, the next stacked box still in front of the best hit, or none
 // (T.cur = -1).
-__device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T, uint2* stack,
+template <class Stack>
+__device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T, Stack& stack,
                                          BvhCounters& cnt) {
     const float4* np = bv.nodes[T.cur].v;
     float4 lo[4], hi[4];
@@ -227,15 +259,15 @@ __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, boo
     bvh_cswap(k1, v1, k2, v2);
     if (k0 != INF) {
         // an entry is (node, entry distance bits): one 8-byte local store or load
-        if (k3 != INF) stack[T.sp++] = make_uint2((unsigned)v3, __float_as_uint(k3));
-        if (k2 != INF) stack[T.sp++] = make_uint2((unsigned)v2, __float_as_uint(k2));
-        if (k1 != INF) stack[T.sp++] = make_uint2((unsigned)v1, __float_as_uint(k1));
+        if (k3 != INF) stack.push(T.sp, make_uint2((unsigned)v3, __float_as_uint(k3)));
+        if (k2 != INF) stack.push(T.sp, make_uint2((unsigned)v2, __float_as_uint(k2)));
+        if (k1 != INF) stack.push(T.sp, make_uint2((unsigned)v1, __float_as_uint(k1)));
         T.cur = v0;
     } else {
         // pop the next box still in front of the best hit
         int next = -1;
         while (T.sp > 0) {
-            const uint2 top = stack[--T.sp];
+            const uint2 top = stack.pop(T.sp);
             if (__uint_as_float(top.y) <= lim) {
                 next = (int)top.x;
                 break;
@@ -258,7 +290,8 @@ __device__ __forceinline__ void bvh_leaf_step(const BvhView& bv, const RayPre& r
 // Closest hit through the BVH: the same (t, index) the brute-force loop gives.
 __device__ __forceinline__ void bvh_intersect(const BvhView& bv, const RayPre& r, bool fast, float& best, int& bidx,
                                               BvhCounters& cnt) {
-    uint2 stack[kBvhStack];
+    uint2 st[kBvhStack];
+    LocalStack stack{st};
     BvhTrav T;
     bvh_begin(bv, r, fast, T, cnt);
     while (T.cur >= 0 || T.lmask != 0u) {

@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const bool scene_fast = P.sc.fast_div != 0u;
-    uint2 stack[kBvhStack];
+    extern __shared__ uint2 s_stack[];  // kShortStack entries per thread
+    uint2 deep[kBvhStack - kShortStack];
+    SplitStack stack{s_stack + threadIdx.x, blockDim.x, deep};
     BvhCounters cnt;
     BvhTrav T;
     T.cur = -1;
@@ -506,13 +508,16 @@ cudaError_t launch_render(const RenderParams& p, int grid, int block, size_t sme
     return cudaGetLastError();
 }
 
+size_t render_bvh_smem_bytes(int block) { return (size_t)block * kShortStack * sizeof(uint2); }
+
 cudaError_t launch_render_bvh(const RenderParams& p, int grid, int block, cudaStream_t s) {
-    render_bvh_kernel<<<grid, block, 0, s>>>(p);
+    render_bvh_kernel<<<grid, block, render_bvh_smem_bytes(block), s>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t render_bvh_occupancy(int block, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, render_bvh_kernel, block, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, render_bvh_kernel, block,
+                                                         render_bvh_smem_bytes(block));
 }
 
 cudaError_t render_occupancy(int block, size_t smem, int* blocks_per_sm) {
