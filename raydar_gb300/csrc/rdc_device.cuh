@@ -168,6 +168,8 @@ struct RayPre {
     V3 rd;     // RN(1/d) per component
     bool fast; // operands inside the exact-reciprocal-division range
     float2 nz; // (-0, -0), opaque to the compiler (see mul2)
+    float P;   // 2^-15 a oo: the per-ray part of the sphere filter's margin
+    float ol1; // |o.x| + |o.y| + |o.z| >= |o|: the cube filter's growth
 };
 
 __device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float2 nz) {
@@ -179,6 +181,8 @@ __device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float2 nz) {
     r.od = vdot(o, d);
     r.oo = vdot(o, o);
     r.ra = __frcp_rn(r.a);
+    r.P = (r.a * 3.0517578e-05f /* 2^-15 */) * r.oo;
+    r.ol1 = (fabsf(o.x) + fabsf(o.y)) + fabsf(o.z);
     r.rd = mk(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
     const float D0 = 9.094947e-13f /* 2^-40 */, D1 = 16.0f;
     const float O0 = 8.6736174e-19f /* 2^-60 */, O1 = 1.1258999e15f /* 2^50 */;
@@ -196,55 +200,81 @@ __device__ __forceinline__ float sphere_div(float num, const RayPre& r) {
     return num / r.a;
 }
 
-// hit_sphere (src/renderer/cpu.rs:34-62), pass 1: the discriminant of up to
-// 32 spheres of a run (packed pairs, rdc_flatten.hpp), two per instruction,
-// into a bit mask of the spheres that can return a hit.  disc < 0 returns
-// None in the reference.  With the fast (guarded) arithmetic a sphere whose
-// whole line intersection lies behind the origin is dropped too: k >= 2^-63
-// (k*k normal) and disc < k*k*(1 - 2^-20) force RN(sqrt(disc)) < k, so both
-// roots are negative and the reference returns None.
+// hit_sphere (src/renderer/cpu.rs:34-62), pass 1: a bit mask of the spheres
+// of a run (up to 32, packed pairs, rdc_flatten.hpp) that can return a hit,
+// two spheres per instruction.  Pass 2 (sphere_exact) decides each
+// candidate with the reference's own arithmetic, so pass 1 only has to be
+// conservative: it may keep a sphere the reference misses, never drop one
+// it hits.
+//
+// Exact pass 1 (Fast = false): the reference's discriminant itself; disc < 0
+// (sign bit set: disc is never -0 since k*k >= +0) returns None.
+//
+// Filter (Fast = true, range-guarded operands: no overflow, a >= 2^-34):
+// with w = o - c, b = w.d and e = |w|^2 - q as FMA chains, where q = r^2 +
+// 2^-16 (2 c.c + r^2) + 2^-70 rounded up (flatten), and P = 2^-15 a o.o per
+// ray, the filter's discriminant is disc' = RN(b^2 + RN(P - a e)).  Exactly,
+// b^2 - a(|w|^2 - r^2) = A (r^2 - rho^2) = Q (Lagrange's identity; A = d.d,
+// rho the distance from c to the ray's line).  With u = 2^-24 and S = |o| +
+// |c|, first-order rounding bounds: the reference's disc is within
+// u A (21 S^2 + 6 r^2) of Q; the filter's b within 4u sqrt(A) S of the exact
+// w.d and of the reference's k, e within 5u S^2 + 3u q of |w|^2 - q; so
+// disc' >= disc_ref + M - u A (38 S^2 + 13 r^2), where the margin M = A (q -
+// r^2) + P >= 256u A (S^2 + r^2) (2 c.c + 2 o.o >= S^2).  Hence
+// disc' >= disc_ref + 32u A S^2: disc_ref >= 0 keeps the sphere.  The same
+// slack drops a sphere wholly behind the origin: b >= 0 and disc' <
+// b RN(b C), C = 1 - 2^-20, give (the 32u A S^2 covering |k - b| <= 8u
+// sqrt(A) S, and M >= a 2^-70 making k >= 2^-63 normal) disc_ref <
+// k^2 C (1 + 2u), so RN(sqrt(disc_ref)) < k and both of the reference's
+// roots are negative.  13 lane operations per sphere against the exact
+// pass's 21; the filter keeps spheres passing within about
+// sqrt(r^2 + 2^-16 (2|o|^2 + 2|c|^2 + r^2)) of the line, a band far
+// narrower than the spheres themselves at the scales scenes use.
 template <bool Fast>
 __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__ pr, int n,
                                                       const RayPre& r) {
     const float2 dx = f2(r.d.x, r.d.x), dy = f2(r.d.y, r.d.y), dz = f2(r.d.z, r.d.z);
     const float2 ox = f2(r.o.x, r.o.x), oy = f2(r.o.y, r.o.y), oz = f2(r.o.z, r.o.z);
-    const float2 od = f2(r.od, r.od), oo = f2(r.oo, r.oo), a = f2(r.a, r.a);
-    const float CULL = 0.99999905f;                     // 1 - 2^-20
-    const float2 ntiny = f2(-1.0842022e-19f, -1.0842022e-19f);  // -2^-63
     // Each sphere's decision is the sign bit of a word (clear = candidate),
     // shifted into the mask with one funnel shift: sphere j of the chunk ends
-    // at bit n-1-j.  disc is never -0 (k*k >= +0), so sign(disc) is exactly
-    // `disc < 0`; NaN signs only ever add candidates, which pass 2 rejects.
+    // at bit n-1-j.  NaN signs only ever add candidates, which pass 2 rejects.
     uint32_t m = 0;
     const int np = (n + 1) >> 1;
+    if (Fast) {
+        const float2 na = f2(-r.a, -r.a), P = f2(r.P, r.P);
+        const float2 nC = f2(-0.99999905f, -0.99999905f);  // -(1 - 2^-20)
 #pragma unroll 4
-    for (int p = 0; p < np; ++p) {
-        const float4 A = pr[3 * p];
-        const float4 B = pr[3 * p + 1];
-        const float2 rr = *reinterpret_cast<const float2*>(&pr[3 * p + 2]);
-        const float2 cx = f2(A.x, A.y), cy = f2(A.z, A.w), cz = f2(B.x, B.y), cc = f2(B.z, B.w);
-        const float2 dc = add2(add2(mul2(dx, cx, r.nz), mul2(dy, cy, r.nz)), mul2(dz, cz, r.nz));
-        const float2 k = sub2(od, dc);
-        const float2 oc = add2(add2(mul2(ox, cx, r.nz), mul2(oy, cy, r.nz)), mul2(oz, cz, r.nz));
-        const float2 c = sub2(add2(sub2(oo, add2(oc, oc)), cc), rr);
-        const float2 kk = mul2(k, k, r.nz);
-        const float2 disc = sub2(kk, mul2(a, c, r.nz));
-        uint32_t w0, w1;
-        if (Fast) {
-            // cull (k >= 2^-63 and disc < lim) from the signs of k - 2^-63 and
-            // disc - lim, both exact in sign (finite operands: range guards).
-            const float2 lim = mul2(kk, f2(CULL, CULL), r.nz);
-            const float2 kd = add2(k, ntiny);
-            const float2 ld = sub2(disc, lim);
-            // keep = ~s_disc & (s_kd | ~s_ld): bit 31 clear <=> candidate
-            w0 = ~(~__float_as_uint(disc.x) & (__float_as_uint(kd.x) | ~__float_as_uint(ld.x)));
-            w1 = ~(~__float_as_uint(disc.y) & (__float_as_uint(kd.y) | ~__float_as_uint(ld.y)));
-        } else {
-            w0 = __float_as_uint(disc.x);
-            w1 = __float_as_uint(disc.y);
+        for (int p = 0; p < np; ++p) {
+            const float4 A = pr[3 * p];
+            const float4 B = pr[3 * p + 1];
+            const float2 wx = sub2(ox, f2(A.x, A.y)), wy = sub2(oy, f2(A.z, A.w)), wz = sub2(oz, f2(B.x, B.y));
+            const float2 b = fma2(wz, dz, fma2(wy, dy, mul2(wx, dx, r.nz)));
+            const float2 e = fma2(wz, wz, fma2(wy, wy, fma2(wx, wx, f2(B.z, B.w))));  // B.zw = -q
+            const float2 disc = fma2(b, b, fma2(na, e, P));
+            const float2 ld = fma2(mul2(b, nC, r.nz), b, disc);  // disc' - b RN(b C), sign exact
+            // keep = ~s_disc & (s_b | ~s_ld): bit 31 clear <=> candidate
+            const uint32_t w0 = ~(~__float_as_uint(disc.x) & (__float_as_uint(b.x) | ~__float_as_uint(ld.x)));
+            const uint32_t w1 = ~(~__float_as_uint(disc.y) & (__float_as_uint(b.y) | ~__float_as_uint(ld.y)));
+            m = __funnelshift_l(~w0, m, 1);
+            m = __funnelshift_l(~w1, m, 1);
         }
-        m = __funnelshift_l(~w0, m, 1);
-        m = __funnelshift_l(~w1, m, 1);
+    } else {
+        const float2 od = f2(r.od, r.od), oo = f2(r.oo, r.oo), a = f2(r.a, r.a);
+#pragma unroll 4
+        for (int p = 0; p < np; ++p) {
+            const float4 A = pr[3 * p];
+            const float4 B = pr[3 * p + 1];
+            const float4 C = pr[3 * p + 2];
+            const float2 cx = f2(A.x, A.y), cy = f2(A.z, A.w), cz = f2(B.x, B.y);
+            const float2 cc = f2(C.x, C.y), rr = f2(C.z, C.w);
+            const float2 dc = add2(add2(mul2(dx, cx, r.nz), mul2(dy, cy, r.nz)), mul2(dz, cz, r.nz));
+            const float2 k = sub2(od, dc);
+            const float2 oc = add2(add2(mul2(ox, cx, r.nz), mul2(oy, cy, r.nz)), mul2(oz, cz, r.nz));
+            const float2 c = sub2(add2(sub2(oo, add2(oc, oc)), cc), rr);
+            const float2 disc = sub2(mul2(k, k, r.nz), mul2(a, c, r.nz));
+            m = __funnelshift_l(~__float_as_uint(disc.x), m, 1);
+            m = __funnelshift_l(~__float_as_uint(disc.y), m, 1);
+        }
     }
     if (2 * np > n) m >>= 1;  // drop the padding half of an odd chunk
     return m;
@@ -258,7 +288,7 @@ template <bool Fast>
 __device__ __forceinline__ void sphere_exact(const float4* __restrict__ pr, int j, int obj,
                                              const RayPre& r, float& best, int& bidx) {
     const float* q = reinterpret_cast<const float*>(pr + 3 * (j >> 1)) + (j & 1);
-    const float cx = q[0], cy = q[2], cz = q[4], cc = q[6], rr = q[8];
+    const float cx = q[0], cy = q[2], cz = q[4], cc = q[8], rr = q[10];
     const float dc = (r.d.x * cx + r.d.y * cy) + r.d.z * cz;
     const float k = r.od - dc;
     const float oc = (r.o.x * cx + r.o.y * cy) + r.o.z * cz;
@@ -280,14 +310,12 @@ __device__ __forceinline__ void sphere_exact(const float4* __restrict__ pr, int 
 }
 
 // hit_cube, src/renderer/cpu.rs:64-98: the two slab planes of each axis
-// divided as a pair.
+// divided as a pair; X, Y, Z hold (min, max) of each axis.
 template <bool Fast>
-__device__ __forceinline__ void cube_test(const float4* __restrict__ cr, int i, const RayPre& r,
-                                          float& best, int& bidx) {
-    const float4 A = cr[0];
-    const float2 Z = *reinterpret_cast<const float2*>(&cr[1]);
-    const float2 ax = sub2(f2(A.x, A.y), f2(r.o.x, r.o.x));
-    const float2 ay = sub2(f2(A.z, A.w), f2(r.o.y, r.o.y));
+__device__ __forceinline__ void cube_slab(float2 X, float2 Y, float2 Z, int i, const RayPre& r, float& best,
+                                          int& bidx) {
+    const float2 ax = sub2(X, f2(r.o.x, r.o.x));
+    const float2 ay = sub2(Y, f2(r.o.y, r.o.y));
     const float2 az = sub2(Z, f2(r.o.z, r.o.z));
     float2 tx, ty, tz;
     if (Fast) {
@@ -308,6 +336,115 @@ __device__ __forceinline__ void cube_test(const float4* __restrict__ cr, int i, 
             bidx = i;
         }
     }
+}
+
+// The same test on a cube record in the slab pair layout (min.x, max.x,
+// min.y, max.y) (min.z, max.z, ...): the LBVH's primitives.
+template <bool Fast>
+__device__ __forceinline__ void cube_test(const float4* __restrict__ cr, int i, const RayPre& r, float& best,
+                                          int& bidx) {
+    const float4 A = cr[0];
+    const float4 B = cr[1];
+    cube_slab<Fast>(f2(A.x, A.y), f2(A.z, A.w), f2(B.x, B.y), i, r, best, bidx);
+}
+
+// The same test on cube j of a brute-force chunk (pairs of cubes, rdc_flatten.hpp:
+// (min.x, min.x', max.x, max.x') and likewise y, z per pair).
+template <bool Fast>
+__device__ __forceinline__ void cube_exact(const float4* __restrict__ pr, int j, int obj, const RayPre& r,
+                                           float& best, int& bidx) {
+    const float* q = reinterpret_cast<const float*>(pr + 3 * (j >> 1)) + (j & 1);
+    cube_slab<Fast>(f2(q[0], q[2]), f2(q[4], q[6]), f2(q[8], q[10]), obj, r, best, bidx);
+}
+
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// hit_cube pass 1 on the guarded fast path: a conservative filter, the
+// LBVH's box test (rdc_bvh.cuh) on every cube of a chunk (up to 32, two per
+// packed instruction), into a bit mask of the cubes the exact pass 2
+// (cube_exact) has to decide.  A cube is dropped only when the grown box
+// [min - m, max + m] lies wholly behind the origin, is missed, or is entered
+// strictly beyond the best hit so far (the reference replaces only on a
+// strictly smaller t, and best only shrinks within the chunk).  The growth
+// m = 2^-20 (|o| + 2R) + 1e-30, R >= |centre| + half side * sqrt(3) over the
+// run, covers the reference's slab rounding and this test's own (the bound
+// is proven for the LBVH's leaves, which run the same exact test after the
+// same box test).  Per ray, the near and far plane of each axis are known
+// from the sign of 1/d, so each cube takes two plane distances per axis
+// (one FMA each, FMA(plane, 1/d, -(o +- m)/d)) and one three-input max and
+// min; far distances subtract a subtrahend lowered by 2^-120, which never
+// lets them be -0 and keeps `exit >= 0` an exact sign test.
+constexpr int kCubeFilterMinRun = 4;  // shortest cube run the filter is used on
+
+struct CubeFilterRay {
+    float2 inv[3];    // RN(1/d) per axis, both halves
+    float2 nnear[3];  // -(o + m)/d or -(o - m)/d: the near plane's subtrahend, negated
+    float2 nfar[3];   // the far plane's, negated and raised by 2^-120
+    int near_off[3];  // float2 index of the near planes within the axis's float4: 0 (min) or 1 (max)
+};
+
+__device__ __forceinline__ CubeFilterRay cube_filter_ray(const RayPre& r, float R) {
+    CubeFilterRay c;
+    const float m = 9.536743e-7f /* 2^-20 */ * (r.ol1 + 2.0f * R) + 1e-30f;
+    const float o[3] = {r.o.x, r.o.y, r.o.z};
+    const float inv[3] = {r.rd.x, r.rd.y, r.rd.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float oa = (o[k] + m) * inv[k];  // subtrahend of the min plane
+        const float ob = (o[k] - m) * inv[k];  // of the max plane
+        const bool pos = inv[k] >= 0.0f;
+        const float nn = -(pos ? oa : ob);
+        const float nf = 7.5231638e-37f /* 2^-120 */ - (pos ? ob : oa);
+        c.inv[k] = f2(inv[k], inv[k]);
+        c.nnear[k] = f2(nn, nn);
+        c.nfar[k] = f2(nf, nf);
+        c.near_off[k] = pos ? 0 : 1;
+    }
+    return c;
+}
+
+// Plane distances of the two cubes of a pair, one packed FMA.
+__device__ __forceinline__ float2 cube_planes(float2 p, float2 inv, float2 ns) { return fma2(p, inv, ns); }
+
+__device__ __forceinline__ uint32_t cube_candidates(const float4* __restrict__ pr, int n, const CubeFilterRay& c,
+                                                    float best) {
+    const float2* p2 = reinterpret_cast<const float2*>(pr);
+    const float2* nx = p2 + c.near_off[0];
+    const float2* fx = p2 + (1 - c.near_off[0]);
+    const float2* ny = p2 + 2 + c.near_off[1];
+    const float2* fy = p2 + 2 + (1 - c.near_off[1]);
+    const float2* nz = p2 + 4 + c.near_off[2];
+    const float2* fz = p2 + 4 + (1 - c.near_off[2]);
+    const float2 b2 = f2(best, best);
+    uint32_t m = 0;
+    const int np = (n + 1) >> 1;
+#pragma unroll 2
+    for (int p = 0; p < np; ++p) {
+        const int o = 6 * p;
+        const float2 ex = cube_planes(nx[o], c.inv[0], c.nnear[0]), xx = cube_planes(fx[o], c.inv[0], c.nfar[0]);
+        const float2 ey = cube_planes(ny[o], c.inv[1], c.nnear[1]), xy = cube_planes(fy[o], c.inv[1], c.nfar[1]);
+        const float2 ez = cube_planes(nz[o], c.inv[2], c.nnear[2]), xz = cube_planes(fz[o], c.inv[2], c.nfar[2]);
+        const float2 entry = f2(fmax3(ex.x, ey.x, ez.x), fmax3(ex.y, ey.y, ez.y));
+        const float2 exit = f2(fmin3(xx.x, xy.x, xz.x), fmin3(xx.y, xy.y, xz.y));
+        const float2 span = sub2(exit, entry);  // exit >= entry
+        const float2 lead = sub2(b2, entry);    // entry <= best
+        // bit 31 set <=> dropped (exit < 0, exit < entry or entry > best)
+        const uint32_t w0 = __float_as_uint(span.x) | __float_as_uint(lead.x) | __float_as_uint(exit.x);
+        const uint32_t w1 = __float_as_uint(span.y) | __float_as_uint(lead.y) | __float_as_uint(exit.y);
+        m = __funnelshift_l(~w0, m, 1);
+        m = __funnelshift_l(~w1, m, 1);
+    }
+    if (2 * np > n) m >>= 1;  // drop the padding half of an odd chunk
+    return m;
 }
 
 // Brute-force closest hit over all objects in scene order.
@@ -332,9 +469,26 @@ __device__ __forceinline__ void intersect_runs(const float4* __restrict__ rec,
                 }
             }
         } else {
-            const float4* cr = rec + run.w;
-#pragma unroll 2
-            for (int i = run.y; i < run.z; ++i) cube_test<Fast>(cr + 2 * (i - run.y), i, r, best, bidx);
+            // a cube run: a header (R, 0, 0, 0), then 3 float4 per pair of cubes
+            const float4* pr0 = rec + run.w + 1;
+            // the filter's per-ray setup pays off from a few cubes on (a
+            // lone ground cube, which most rays hit, goes straight to pass 2)
+            if (Fast && run.z - run.y >= kCubeFilterMinRun) {
+                const CubeFilterRay c = cube_filter_ray(r, rec[run.w].x);
+                for (int cb = run.y; cb < run.z; cb += 32) {
+                    const int n = min(32, run.z - cb);
+                    const float4* pr = pr0 + 3 * ((cb - run.y) >> 1);
+                    uint32_t m = cube_candidates(pr, n, c, best);
+                    while (m != 0u) {  // highest bit first = scene order
+                        const int pos = 31 - __clz(m);
+                        m ^= 1u << pos;
+                        const int j = n - 1 - pos;
+                        cube_exact<Fast>(pr, j, cb + j, r, best, bidx);
+                    }
+                }
+            } else {
+                for (int i = run.y; i < run.z; ++i) cube_exact<Fast>(pr0, i - run.y, i, r, best, bidx);
+            }
         }
     }
 }
