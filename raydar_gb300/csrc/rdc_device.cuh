@@ -210,26 +210,27 @@ __device__ __forceinline__ float sphere_div(float num, const RayPre& r) {
 // Exact pass 1 (Fast = false): the reference's discriminant itself; disc < 0
 // (sign bit set: disc is never -0 since k*k >= +0) returns None.
 //
-// Filter (Fast = true, range-guarded operands: no overflow, a >= 2^-34):
-// with w = o - c, b = w.d and e = |w|^2 - q as FMA chains, where q = r^2 +
-// 2^-16 (2 c.c + r^2) + 2^-70 rounded up (flatten), and P = 2^-15 a o.o per
-// ray, the filter's discriminant is disc' = RN(b^2 + RN(P - a e)).  Exactly,
-// b^2 - a(|w|^2 - r^2) = A (r^2 - rho^2) = Q (Lagrange's identity; A = d.d,
-// rho the distance from c to the ray's line).  With u = 2^-24 and S = |o| +
-// |c|, first-order rounding bounds: the reference's disc is within
-// u A (21 S^2 + 6 r^2) of Q; the filter's b within 4u sqrt(A) S of the exact
-// w.d and of the reference's k, e within 5u S^2 + 3u q of |w|^2 - q; so
-// disc' >= disc_ref + M - u A (38 S^2 + 13 r^2), where the margin M = A (q -
-// r^2) + P >= 256u A (S^2 + r^2) (2 c.c + 2 o.o >= S^2).  Hence
-// disc' >= disc_ref + 32u A S^2: disc_ref >= 0 keeps the sphere.  The same
-// slack drops a sphere wholly behind the origin: b >= 0 and disc' <
-// b RN(b C), C = 1 - 2^-20, give (the 32u A S^2 covering |k - b| <= 8u
-// sqrt(A) S, and M >= a 2^-70 making k >= 2^-63 normal) disc_ref <
-// k^2 C (1 + 2u), so RN(sqrt(disc_ref)) < k and both of the reference's
-// roots are negative.  13 lane operations per sphere against the exact
-// pass's 21; the filter keeps spheres passing within about
-// sqrt(r^2 + 2^-16 (2|o|^2 + 2|c|^2 + r^2)) of the line, a band far
-// narrower than the spheres themselves at the scales scenes use.
+// Filter (Fast = true, range-guarded operands: no overflow, a >= 2^-34): as
+// FMA chains, b = o.d - c.d (from the reference's own o.d) and e = (o.o + s)
+// - 2 o.c, where s = c.c - q rounded down and q = r^2 + 2^-16 (2 c.c + r^2)
+// + 2^-70 rounded up (flatten), and P = 2^-15 a o.o per ray; the filter's
+// discriminant is disc' = RN(b^2 + RN(P - a e)).  Exactly, with w = o - c,
+// b = w.d and e = |w|^2 - q, and b^2 - a(|w|^2 - r^2) = A (r^2 - rho^2) = Q
+// (Lagrange's identity; A = d.d, rho the distance from c to the ray's line).
+// With u = 2^-24 and S = |o| + |c|, first-order rounding bounds: the
+// reference's disc is within u A (21 S^2 + 6 r^2) of Q; the filter's b within
+// 6u sqrt(A) S of w.d and 10u sqrt(A) S of the reference's k, e within
+// 8u S^2 + 5u q of |w|^2 - q; so disc' >= disc_ref + M - u A (45 S^2 +
+// 15 r^2), where the margin M = A (q - r^2) + P >= 256u A (S^2 + r^2)
+// (2 c.c + 2 o.o >= S^2).  Hence disc' >= disc_ref + 40u A S^2: disc_ref >= 0
+// keeps the sphere.  The same slack drops a sphere wholly behind the origin:
+// b >= 0 and disc' < b RN(b C), C = 1 - 2^-20, give (40u A S^2 covering
+// 2 b |k - b|, and M >= a 2^-70 making k >= 2^-63 normal) disc_ref <
+// k^2 C (1 + 2u), so RN(sqrt(disc_ref)) < k and both of the reference's roots
+// are negative.  11 lane operations per sphere against the exact pass's 21;
+// the filter keeps spheres passing within about sqrt(r^2 + 2^-16 (2|o|^2 +
+// 2|c|^2 + r^2)) of the line, a band far narrower than the spheres
+// themselves at the scales scenes use.
 template <bool Fast>
 __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__ pr, int n,
                                                       const RayPre& r) {
@@ -243,13 +244,17 @@ __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__
     if (Fast) {
         const float2 na = f2(-r.a, -r.a), P = f2(r.P, r.P);
         const float2 nC = f2(-0.99999905f, -0.99999905f);  // -(1 - 2^-20)
+        const float2 od = f2(r.od, r.od), oo = f2(r.oo, r.oo);
+        const float2 ndx = f2(-r.d.x, -r.d.x), ndy = f2(-r.d.y, -r.d.y), ndz = f2(-r.d.z, -r.d.z);
+        const float2 mx = f2(-2.0f * r.o.x, -2.0f * r.o.x), my = f2(-2.0f * r.o.y, -2.0f * r.o.y),
+                     mz = f2(-2.0f * r.o.z, -2.0f * r.o.z);
 #pragma unroll 4
         for (int p = 0; p < np; ++p) {
             const float4 A = pr[3 * p];
             const float4 B = pr[3 * p + 1];
-            const float2 wx = sub2(ox, f2(A.x, A.y)), wy = sub2(oy, f2(A.z, A.w)), wz = sub2(oz, f2(B.x, B.y));
-            const float2 b = fma2(wz, dz, fma2(wy, dy, mul2(wx, dx, r.nz)));
-            const float2 e = fma2(wz, wz, fma2(wy, wy, fma2(wx, wx, f2(B.z, B.w))));  // B.zw = -q
+            const float2 cx = f2(A.x, A.y), cy = f2(A.z, A.w), cz = f2(B.x, B.y);
+            const float2 b = fma2(ndz, cz, fma2(ndy, cy, fma2(ndx, cx, od)));
+            const float2 e = fma2(mz, cz, fma2(my, cy, fma2(mx, cx, add2(oo, f2(B.z, B.w)))));  // B.zw = s
             const float2 disc = fma2(b, b, fma2(na, e, P));
             const float2 ld = fma2(mul2(b, nC, r.nz), b, disc);  // disc' - b RN(b C), sign exact
             // keep = ~s_disc & (s_b | ~s_ld): bit 31 clear <=> candidate

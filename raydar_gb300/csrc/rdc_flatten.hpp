@@ -5,8 +5,9 @@
 //   rec[]   float4 records the intersection loop stages in shared memory:
 //           per sphere run, pairs of consecutive spheres (packed for the
 //           kernels' two-wide float instructions), 3 float4 per pair
-//             (c1.x, c2.x, c1.y, c2.y) (c1.z, c2.z, -q1, -q2) (c1.c1, c2.c2, r1*r1, r2*r2)
-//           q the sphere filter's margin-widened r^2 (sphere_filter_q)
+//             (c1.x, c2.x, c1.y, c2.y) (c1.z, c2.z, s1, s2) (c1.c1, c2.c2, r1*r1, r2*r2)
+//           s = c.c - q rounded down, q the sphere filter's margin-widened
+//           r^2 (sphere_filter_s)
 //           (an odd run's last pair repeats its sphere in the second half;
 //           the kernel masks that half out);
 //           per cube run, a header (R, 0, 0, 0) with R >= |centre| + half
@@ -73,14 +74,17 @@ inline MatDev flat_material(const rdc_object& o) {
     return md;
 }
 
-// The sphere filter's widened r^2 (sphere_candidates, rdc_device.cuh):
-// q >= r^2 + 2^-16 (2 c.c + r^2) + 2^-70, computed in double and rounded up
-// to float.
-inline float sphere_filter_q(const float c[3], float rr) {
+// The sphere filter's per-sphere constant (sphere_candidates,
+// rdc_device.cuh): s <= c.c - q with q >= r^2 + 2^-16 (2 c.c + r^2) + 2^-70,
+// computed in double (c.c and q within 2^-51 relative of exact, far inside
+// the 2^-50 (c.c + q) subtracted) and rounded down to float.
+inline float sphere_filter_s(const float c[3], float rr) {
     const double cc = (double)c[0] * c[0] + (double)c[1] * c[1] + (double)c[2] * c[2];
     const double q = ((double)rr + std::ldexp(2.0 * cc + (double)rr, -16) + 0x1p-70) * (1.0 + 0x1p-40);
-    float f = (float)q;
-    if ((double)f < q) f = std::nextafter(f, INFINITY);
+    const double v = cc - q;
+    const double s = v - std::fabs(v) * 0x1p-45 - std::ldexp(cc + q, -50);
+    float f = (float)s;
+    if ((double)f > s) f = std::nextafter(f, -INFINITY);
     return f;
 }
 
@@ -122,7 +126,7 @@ inline bool flatten(const rdc_scene_desc* sc, float4* rec, float4* hit, MatDev* 
                 const float cc2 = (c2[0] * c2[0] + c2[1] * c2[1]) + c2[2] * c2[2];
                 const float rr1 = s1.radius * s1.radius, rr2 = s2.radius * s2.radius;
                 rec[off++] = make_float4(c1[0], c2[0], c1[1], c2[1]);
-                rec[off++] = make_float4(c1[2], c2[2], -sphere_filter_q(c1, rr1), -sphere_filter_q(c2, rr2));
+                rec[off++] = make_float4(c1[2], c2[2], sphere_filter_s(c1, rr1), sphere_filter_s(c2, rr2));
                 rec[off++] = make_float4(cc1, cc2, rr1, rr2);
                 fast_div = fast_div && sphere_fast_ok(s1.center, s1.radius) && sphere_fast_ok(s2.center, s2.radius);
             }

@@ -40,26 +40,30 @@ def _reference_hits(o, d, c, r):
     return (disc >= 0) & ((t1 >= 0) | (t2 >= 0))
 
 
-def _filter_q(c, rr):
-    """rdc_flatten.hpp sphere_filter_q: r^2 + 2^-16 (2 c.c + r^2) + 2^-70, rounded up."""
+def _filter_s(c, rr):
+    """rdc_flatten.hpp sphere_filter_s: c.c - q rounded down, q = r^2 + 2^-16 (2 c.c + r^2) + 2^-70."""
     cd = c.astype(np.float64)
-    q = (rr.astype(np.float64) + np.ldexp(2.0 * (cd * cd).sum(1) + rr, -16) + 2.0 ** -70) * (1.0 + 2.0 ** -40)
-    f = q.astype(F)
-    low = f.astype(np.float64) < q
-    f[low] = np.nextafter(f[low], F(np.inf))
+    cc = (cd * cd).sum(1)
+    q = (rr.astype(np.float64) + np.ldexp(2.0 * cc + rr, -16) + 2.0 ** -70) * (1.0 + 2.0 ** -40)
+    v = cc - q
+    sd = v - np.abs(v) * 2.0 ** -45 - np.ldexp(cc + q, -50)
+    f = sd.astype(F)
+    high = f.astype(np.float64) > sd
+    f[high] = np.nextafter(f[high], F(-np.inf))
     return f
 
 
 def _filter_keeps(o, d, c, r):
     """sphere_candidates<true> (rdc_device.cuh), one sphere per row."""
     rr = r * r
-    nq = -_filter_q(c, rr)
+    s_ = _filter_s(c, rr)
     a = _dot(d, d)
     oo = _dot(o, o)
+    od = _dot(o, d)
     P = (a * F(2.0 ** -15)) * oo
-    w = o - c
-    b = _fma(w[:, 2], d[:, 2], _fma(w[:, 1], d[:, 1], w[:, 0] * d[:, 0]))
-    e = _fma(w[:, 2], w[:, 2], _fma(w[:, 1], w[:, 1], _fma(w[:, 0], w[:, 0], nq)))
+    b = _fma(-d[:, 2], c[:, 2], _fma(-d[:, 1], c[:, 1], _fma(-d[:, 0], c[:, 0], od)))
+    m2o = F(-2) * o
+    e = _fma(m2o[:, 2], c[:, 2], _fma(m2o[:, 1], c[:, 1], _fma(m2o[:, 0], c[:, 0], oo + s_)))
     disc = _fma(b, b, _fma(-a, e, P))
     ld = _fma(b * F(-0.99999905), b, disc)
     s = lambda x: np.signbit(x)
