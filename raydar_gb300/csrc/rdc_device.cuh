@@ -771,6 +771,23 @@ __device__ __forceinline__ void path_start(const SceneView& sc, uint32_t pix, Pa
     s.bounce = 0;
 }
 
+// The next sample of the same pixel: the primary ray is a function of the
+// pixel alone (the same floats every sample), so the kernels keep its
+// direction in a per-thread shared-memory slot (`dir`, written after
+// path_start) instead of recomputing it (six IEEE divisions and a
+// normalisation per sample).
+__device__ __forceinline__ void path_keep(const PathState& s, float4* dir) {
+    *dir = make_float4(s.d.x, s.d.y, s.d.z, 0.0f);
+}
+__device__ __forceinline__ void path_restart(const SceneView& sc, const float4* dir, PathState& s) {
+    const float4 d = *dir;
+    s.o = mk(sc.cam_pos[0], sc.cam_pos[1], sc.cam_pos[2]);
+    s.d = mk(d.x, d.y, d.z);
+    s.atten = mk(1.f, 1.f, 1.f);
+    s.light = mk(0.f, 0.f, 0.f);
+    s.bounce = 0;
+}
+
 // Brute-force closest hit over a scene's records (shared or global memory).
 struct BruteIsect {
     const float4* rec;

@@ -21,7 +21,7 @@ namespace rdc {
 
 // The persistent per-lane loop over the pixel pool (see the file comment).
 template <class Isect>
-__device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& isect) {
+__device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& isect, float4* pdir) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int pix = -1;
@@ -49,6 +49,7 @@ __device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& is
                     pix = (int)mine;
                     acc = P.accum[pix];
                     path_start(P.sc, mine, st);
+                    path_keep(st, pdir);
                     sample = P.s0;
                     send = P.s0 + P.nspp;
                 }
@@ -68,9 +69,7 @@ __device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& is
                 P.accum[pix] = acc;
                 pix = -1;
             } else {
-                // Next sample of the same pixel: the primary ray is recomputed
-                // (identical every sample) rather than kept in registers.
-                path_start(P.sc, (uint32_t)pix, st);
+                path_restart(P.sc, pdir, st);  // next sample of the same pixel
             }
         }
     }
@@ -92,8 +91,9 @@ __global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderPar
     if (threadIdx.x == 0) bulk_init(&s_bar);
     __syncthreads();
     if (!stage_scene(&s_bar, 0u, s_rec, P.sc.rec, P.sc.nrec, s_runs, P.sc.runs, P.sc.nruns, P.errors)) return;
+    __shared__ float4 s_pdir[kRenderBlock];  // each thread's pixel's primary direction
     BruteIsect isect{s_rec, s_runs, (int)P.sc.nruns, P.sc.fast_div != 0u};
-    const uint32_t segs = render_loop(P, isect);
+    const uint32_t segs = render_loop(P, isect, &s_pdir[threadIdx.x]);
     add_warp_sum(P.segments, segs);
 }
 
@@ -120,6 +120,8 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
     const int lane = threadIdx.x & 31;
     const bool scene_fast = P.sc.fast_div != 0u;
     extern __shared__ uint2 s_stack[];  // kShortStack entries per thread
+    __shared__ float4 s_pdir[kRenderBlock];  // each thread's pixel's primary direction
+    float4* const pdir = &s_pdir[threadIdx.x];
     uint2 deep[kBvhStack - kShortStack];
     SplitStack stack{s_stack + threadIdx.x, blockDim.x, deep};
     BvhCounters cnt;
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
                     in_flight = false;
                     return;
                 }
-                path_start(P.sc, (uint32_t)pix, st);
+                path_restart(P.sc, pdir, st);
             }
             if (st.bounce >= P.max_bounces) {  // max_bounces == 0: the path adds (0, 0, 0, 1)
                 ended = true;
@@ -197,6 +199,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
                     pix = (int)mine;
                     acc = P.accum[pix];
                     path_start(P.sc, mine, st);
+                    path_keep(st, pdir);
                     sample = P.s0;
                     send = P.s0 + P.nspp;
                     advance(false);
@@ -273,6 +276,8 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
     __shared__ BatchScene s_bs;
     __shared__ int s_scene;
     __shared__ __align__(8) uint64_t s_bar;
+    __shared__ float4 s_pdir[kRenderBlock];  // each thread's pixel's primary direction (block <= kRenderBlock)
+    float4* const pdir = &s_pdir[threadIdx.x];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < 32) {
@@ -325,6 +330,7 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
                         pix = (int)mine;
                         acc = s_bs.accum[pix];
                         path_start(s_bs.sc, mine, st);
+                        path_keep(st, pdir);
                         sample = 0;
                     }
                 }
@@ -343,7 +349,7 @@ __global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParam
                     s_bs.accum[pix] = acc;
                     pix = -1;
                 } else {
-                    path_start(s_bs.sc, (uint32_t)pix, st);
+                    path_restart(s_bs.sc, pdir, st);
                 }
             }
         }
