@@ -432,7 +432,7 @@ __device__ __forceinline__ uint32_t cube_candidates(const float4* __restrict__ p
     const float2 b2 = f2(best, best);
     uint32_t m = 0;
     const int np = (n + 1) >> 1;
-#pragma unroll 2
+#pragma unroll 4
     for (int p = 0; p < np; ++p) {
         const int o = 6 * p;
         const float2 ex = cube_planes(nx[o], c.inv[0], c.nnear[0]), xx = cube_planes(fx[o], c.inv[0], c.nfar[0]);
