@@ -83,7 +83,7 @@ __device__ __forceinline__ void add_warp_sum(unsigned long long* dst, unsigned l
 }
 
 // Brute force: the scene's records are staged in shared memory per block.
-__global__ void __launch_bounds__(kRenderBlock, 4) render_kernel(const RenderParams P) {
+__global__ void __launch_bounds__(kRenderBlock, 3) render_kernel(const RenderParams P) {
     extern __shared__ float4 smem[];
     __shared__ __align__(8) uint64_t s_bar;
     float4* s_rec = smem;
@@ -271,7 +271,7 @@ __device__ __forceinline__ int batch_busiest_scene(const BatchParams& P, int lan
     return best > 0u ? best_s : -1;
 }
 
-__global__ void __launch_bounds__(kRenderBlock, 4) batch_kernel(const BatchParams P) {
+__global__ void __launch_bounds__(kRenderBlock, 3) batch_kernel(const BatchParams P) {
     extern __shared__ float4 smem[];
     __shared__ BatchScene s_bs;
     __shared__ int s_scene;
