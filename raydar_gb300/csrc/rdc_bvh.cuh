@@ -16,7 +16,7 @@
 //     Its sphere test is the expanded quadratic.  With u = 2^-24,
 //     S = |o| + |c| and A = d.d, first-order rounding analysis of
 //     a = d.d, k = o.d - d.c, c = ((o.o - 2 o.c) + c.c) - r^2 and
-//     disc = k^2 - a c gives |disc - A (r^2 - rho^2)| <= u A (21 S^2 + 4 r^2),
+//     disc = k^2 - a c gives |disc - A (r^2 - rho^2)| <= u A (21 S^2 + 6 r^2),
 //     rho the distance from the centre to the ray's line.  A hit can thus be
 //     reported only when rho^2 <= r^2 (1 + 2^-20) + 2^-19 S^2.  Sphere leaf
 //     boxes are built with that radius for |o| <= o_max (rdc_bvh.cu); a ray
