@@ -69,7 +69,10 @@ __device__ __forceinline__ void bvh_sphere_leaf(const RayPre& r, float4 p0, floa
     const float kk = k * k;
     const float disc = kk - r.a * c;
     if (!(disc >= 0.0f)) return;  // None (NaN too: the reference ends in None)
-    if (Fast && k >= 1.0842022e-19f && disc < kk * 0.99999905f) return;  // both roots behind (proof in rdc_device.cuh)
+    // Both roots behind the origin: k >= 2^-63 keeps k*k normal, and disc <
+    // RN(k*k (1 - 2^-20)) gives sqrt(disc) < k (1 - 2^-21 + 2^-24), so
+    // RN(sqrt(disc)) < k and -k -+ RN(sqrt(disc)) < 0: the reference returns None.
+    if (Fast && k >= 1.0842022e-19f && disc < kk * 0.99999905f) return;
     const float sq = __fsqrt_rn(disc);
     const float t1 = sphere_div<Fast>(-k - sq, r);
     float t = t1;

@@ -238,7 +238,9 @@ __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__
     const float2 ox = f2(r.o.x, r.o.x), oy = f2(r.o.y, r.o.y), oz = f2(r.o.z, r.o.z);
     // Each sphere's decision is the sign bit of a word (clear = candidate),
     // shifted into the mask with one funnel shift: sphere j of the chunk ends
-    // at bit n-1-j.  NaN signs only ever add candidates, which pass 2 rejects.
+    // at bit n-1-j.  A NaN discriminant (possible only off the fast path) is
+    // kept or dropped by its sign bit; either is right, as the reference
+    // returns None for it and pass 2 rejects a kept one.
     uint32_t m = 0;
     const int np = (n + 1) >> 1;
     if (Fast) {

@@ -514,7 +514,7 @@ cudaError_t launch_render(const RenderParams& p, int grid, int block, size_t sme
     return cudaGetLastError();
 }
 
-size_t render_bvh_smem_bytes(int block) { return (size_t)block * kShortStack * sizeof(uint2); }
+static size_t render_bvh_smem_bytes(int block) { return (size_t)block * kShortStack * sizeof(uint2); }
 
 cudaError_t launch_render_bvh(const RenderParams& p, int grid, int block, cudaStream_t s) {
     render_bvh_kernel<<<grid, block, render_bvh_smem_bytes(block), s>>>(p);
