@@ -218,8 +218,13 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
             if (act == 0u || (!first && 32u - (unsigned)__popc(act) >= P.min_idle)) break;
             if (__popc(lm) >= __popc(nm)) {
                 if (wl) bvh_leaf_step(P.bvh, r, rfast, T, cnt);
-            } else {
-                if (wn) bvh_step(P.bvh, r, rfast, T, stack, cnt);
+            } else if (wn) {
+                // up to two node visits per iteration (a lane with no leaves
+                // pending after the first takes the next): half the ballots
+                // and step choices on long node runs (measured +2.6%; three
+                // equal, four slower)
+                bvh_step(P.bvh, r, rfast, T, stack, cnt);
+                if (T.lmask == 0u && T.cur >= 0) bvh_step(P.bvh, r, rfast, T, stack, cnt);
             }
         }
     }
