@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kRenderBlock, 3) adjoint_kernel(const AdjParam
         return;
     float* gbase = P.smem_grad ? s_grad : P.grad;
     const bool scene_fast = P.sc.fast_div != 0u;
-    BruteIsect brute{s_rec, s_runs, (int)P.sc.nruns, scene_fast};
+    BruteIsectRolled brute{s_rec, s_runs, (int)P.sc.nruns, scene_fast};
     BvhCounters cnt;
     uint32_t segs = 0;
 
