@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kRenderBlock, 3) batch_kernel(const BatchParam
             }
             if (__ballot_sync(FULL, pix >= 0) == 0u && !pool_open) break;
             if (pix < 0) continue;
-            BruteIsect isect{s_rec, s_runs, (int)s_bs.sc.nruns, s_bs.sc.fast_div != 0u};
+            BruteIsectRolled isect{s_rec, s_runs, (int)s_bs.sc.nruns, s_bs.sc.fast_div != 0u};
             if (path_segment(s_bs.sc, isect, st, (uint32_t)pix, sample, s_bs.max_bounces,
                              (uint32_t)scene, s_bs.key0, s_bs.key1, segs)) {
                 acc.x = acc.x + st.light.x;
