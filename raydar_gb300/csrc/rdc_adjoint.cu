@@ -184,7 +184,7 @@ __device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7]) {
 }
 
 template <bool kBvh>
-__global__ void __launch_bounds__(kRenderBlock, 3) adjoint_kernel(const AdjParams P) {
+__global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParams P) {
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
     float4* s_rec = smem;
