@@ -64,6 +64,7 @@ def _args():
     p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
     p.add_argument("--no-wavefront", action="store_true", help="skip the megakernel / wavefront A/B")
     p.add_argument("--no-refscene", action="store_true", help="skip the reference's benchmark.rscn at 3840x2160")
+    p.add_argument("--no-progressive", action="store_true", help="skip the editor-style render_sample loop")
     p.add_argument("--wavefront-only", action="store_true", help="only the megakernel / wavefront A/B")
     p.add_argument("--inverse", action="store_true",
                    help="only the config 5 inverse-rendering run (200 Adam steps on 1000 albedos)")
@@ -494,6 +495,40 @@ def reference_scene_bench(local: int, steps: int, spp: int = 16, bounces: int = 
     }
 
 
+def progressive_bench(local: int, samples: int = 256, size: int = 584, bounces: int = 12):
+    """The editor's live view (f1, src/renderer/cpu.rs:142-158 through the
+    reference's render_sample): Scene::default in a 584x584 viewport (the size
+    of the reference's own editor screenshot), one sample per call with the
+    tone-mapped RGBA8 image read back each time, as the editor redraws.  Wall
+    clock per call through the public API (upload check, render, sync,
+    tone map, copy), and the kernel time inside it."""
+    from raydar_gb300 import CudaRenderer, RendererConfig
+    from raydar_gb300.scene import default_scene, resized
+
+    scene = resized(default_scene(), size, size)
+    r = CudaRenderer(RendererConfig(max_sample_count=samples, max_bounces=bounces), device=local, seed=0)
+    r.new_frame(scene)
+    for _ in range(8):  # warm-up: first uploads and launches
+        r.render_sample(scene)
+    r.new_frame(scene)
+    dev_ms, n = 0.0, 0
+    t0 = time.perf_counter()
+    while True:
+        img = r.render_sample(scene)
+        if img is None:
+            break
+        dev_ms += r.stats().device_ms
+        n += 1
+    wall = time.perf_counter() - t0
+    r.close()
+    return {
+        "workload": f"Scene::default at {size}x{size}, {bounces} bounces, {n} calls of render_sample "
+                    f"(1 spp each, RGBA8 read back per call)",
+        "samples_per_s": n / wall, "ms_per_sample_wall": wall / n * 1e3, "kernel_ms_per_sample": dev_ms / n,
+        "d2h_bytes_per_sample": size * size * 4,
+    }
+
+
 def wavefront_bench(local: int, steps: int, spp: int = 64):
     """Megakernel vs wavefront A/B on the headline scene (c2_default 1920x1080,
     12 bounces) at `spp` samples per frame: the same paths, the same
@@ -716,6 +751,10 @@ def run_ours(args):
     if rank == 0 and not args.no_refscene:
         refscene = reference_scene_bench(local, max(1, min(args.steps, 3)))
 
+    progressive = None
+    if rank == 0 and not args.no_progressive:
+        progressive = progressive_bench(local)
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -766,6 +805,7 @@ def run_ours(args):
         "adjoint": adjoint,
         "wavefront_ab": wavefront,
         "reference_benchmark_scene": refscene,
+        "progressive": progressive,
     }
     print(json.dumps(line), flush=True)
 

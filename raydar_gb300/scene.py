@@ -282,6 +282,18 @@ class SceneC:
         return C.byref(self.desc)
 
 
+def resized(scene: Scene, width: int, height: int) -> Scene:
+    """The same scene at another resolution, the camera's matrices recomputed
+    as the reference's Camera setters do (src/scene/camera.rs:140-152): what
+    the editor does when its viewport changes size."""
+    import copy
+    s = copy.deepcopy(scene)
+    s.camera.resolution_x = width
+    s.camera.resolution_y = height
+    s.camera.update_matrices()
+    return s
+
+
 def default_scene() -> Scene:
     """Scene::default (src/scene/mod.rs:20-67)."""
     cam = Camera.new([-3.09, 0.03, -1.16], [0, 0, 0], [0, 1, 0], 854, 480, 0.01, 1000.0, fov=90.0)

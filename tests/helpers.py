@@ -18,11 +18,6 @@ def bits_equal(a, b) -> bool:
 
 
 def shrink(scene, width, height):
-    """Same scene at another resolution, matrices recomputed as the reference's
-    Camera setters do (src/scene/camera.rs:140-152)."""
-    import copy
-    s = copy.deepcopy(scene)
-    s.camera.resolution_x = width
-    s.camera.resolution_y = height
-    s.camera.update_matrices()
-    return s
+    """Same scene at another resolution (raydar_gb300.scene.resized)."""
+    from raydar_gb300.scene import resized
+    return resized(scene, width, height)
