@@ -223,14 +223,12 @@ __device__ __forceinline__ float sphere_div(float num, const RayPre& r) {
 // 8u S^2 + 5u q of |w|^2 - q; so disc' >= disc_ref + M - u A (45 S^2 +
 // 15 r^2), where the margin M = A (q - r^2) + P >= 256u A (S^2 + r^2)
 // (2 c.c + 2 o.o >= S^2).  Hence disc' >= disc_ref + 40u A S^2: disc_ref >= 0
-// keeps the sphere.  The same slack drops a sphere wholly behind the origin:
-// b >= 0 and disc' < b RN(b C), C = 1 - 2^-20, give (40u A S^2 covering
-// 2 b |k - b|, and M >= a 2^-70 making k >= 2^-63 normal) disc_ref <
-// k^2 C (1 + 2u), so RN(sqrt(disc_ref)) < k and both of the reference's roots
-// are negative.  11 lane operations per sphere against the exact pass's 21;
-// the filter keeps spheres passing within about sqrt(r^2 + 2^-16 (2|o|^2 +
-// 2|c|^2 + r^2)) of the line, a band far narrower than the spheres
-// themselves at the scales scenes use.
+// keeps the sphere.  9 lane operations per sphere against the exact pass's
+// 21; the filter keeps spheres passing within about sqrt(r^2 + 2^-16 (2|o|^2
+// + 2|c|^2 + r^2)) of the line, a band far narrower than the spheres
+// themselves at the scales scenes use.  Spheres behind the origin whose line
+// passes that close are kept too and rejected by pass 2: a cull of them here
+// (2 more operations per sphere) measured 9% slower overall.
 template <bool Fast, int Unroll>
 __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__ pr, int n,
                                                       const RayPre& r) {
@@ -245,7 +243,6 @@ __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__
     const int np = (n + 1) >> 1;
     if (Fast) {
         const float2 na = f2(-r.a, -r.a), P = f2(r.P, r.P);
-        const float2 nC = f2(-0.99999905f, -0.99999905f);  // -(1 - 2^-20)
         const float2 od = f2(r.od, r.od), oo = f2(r.oo, r.oo);
         const float2 ndx = f2(-r.d.x, -r.d.x), ndy = f2(-r.d.y, -r.d.y), ndz = f2(-r.d.z, -r.d.z);
         const float2 mx = f2(-2.0f * r.o.x, -2.0f * r.o.x), my = f2(-2.0f * r.o.y, -2.0f * r.o.y),
@@ -258,10 +255,8 @@ __device__ __forceinline__ uint32_t sphere_candidates(const float4* __restrict__
             const float2 b = fma2(ndz, cz, fma2(ndy, cy, fma2(ndx, cx, od)));
             const float2 e = fma2(mz, cz, fma2(my, cy, fma2(mx, cx, add2(oo, f2(B.z, B.w)))));  // B.zw = s
             const float2 disc = fma2(b, b, fma2(na, e, P));
-            const float2 ld = fma2(mul2(b, nC, r.nz), b, disc);  // disc' - b RN(b C), sign exact
-            // keep = ~s_disc & (s_b | ~s_ld): bit 31 clear <=> candidate
-            const uint32_t w0 = ~(~__float_as_uint(disc.x) & (__float_as_uint(b.x) | ~__float_as_uint(ld.x)));
-            const uint32_t w1 = ~(~__float_as_uint(disc.y) & (__float_as_uint(b.y) | ~__float_as_uint(ld.y)));
+            const uint32_t w0 = __float_as_uint(disc.x);
+            const uint32_t w1 = __float_as_uint(disc.y);
             m = __funnelshift_l(~w0, m, 1);
             m = __funnelshift_l(~w1, m, 1);
         }

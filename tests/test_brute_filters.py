@@ -65,9 +65,7 @@ def _filter_keeps(o, d, c, r):
     m2o = F(-2) * o
     e = _fma(m2o[:, 2], c[:, 2], _fma(m2o[:, 1], c[:, 1], _fma(m2o[:, 0], c[:, 0], oo + s_)))
     disc = _fma(b, b, _fma(-a, e, P))
-    ld = _fma(b * F(-0.99999905), b, disc)
-    s = lambda x: np.signbit(x)
-    return ~s(disc) & (s(b) | ~s(ld))
+    return ~np.signbit(disc)
 
 
 def _unit(v):
@@ -112,16 +110,13 @@ def _check(o, d, c, r):
 
 def test_filter_never_drops_a_grazing_hit():
     rng = np.random.default_rng(5)
-    n_hit = n_keep_miss = n_miss = 0
+    n_hit = 0
     for scale_o, scale_c, r_lo, r_hi in CASES:
         for rel in (1e-3, 1e-5, 1e-7):
             o, d, c, r = _grazing(rng, 100_000, scale_o, scale_c, r_lo, r_hi, rel)
-            hit, keep = _check(o, d, c, r)
+            hit, _ = _check(o, d, c, r)
             n_hit += int(hit.sum())
-            n_miss += int((~hit).sum())
-            n_keep_miss += int((keep & ~hit).sum())
-    assert n_hit > 100_000
-    assert n_keep_miss < n_miss  # the band the margin widens stays narrow
+    assert n_hit > 100_000  # (these rays' lines all pass inside the margin band: every one is kept)
 
 
 def test_filter_never_drops_a_hit_from_the_surface():
@@ -134,7 +129,7 @@ def test_filter_never_drops_a_hit_from_the_surface():
     assert n_hit > 10_000  # rounding and inward rays do hit the sphere they leave
 
 
-def test_filter_culls_clear_misses_and_spheres_behind():
+def test_filter_culls_clear_misses():
     rng = np.random.default_rng(7)
     n = 100_000
     c = rng.uniform(-20, 20, (n, 3)).astype(F)
@@ -151,11 +146,14 @@ def test_filter_culls_clear_misses_and_spheres_behind():
     # the margin widens r^2 by 2^-16 (2 |o|^2 + 2 |c|^2 + r^2)
     band = 2.0 ** -16 * (2 * (o.astype(np.float64) ** 2).sum(1) + 2 * (c.astype(np.float64) ** 2).sum(1) + r2)
     far_miss = rho2 > r2 + 1.1 * band
-    behind = (b > 0) & (ww > r2 + 1.1 * band + 2.0 ** -19 * ww)
-    assert far_miss.sum() > n // 2 and behind.sum() > n // 4
+    assert far_miss.sum() > n // 2
     assert not keep[far_miss].any()
-    assert not keep[behind].any()
     assert keep[hit].all()
+    # spheres wholly behind the origin are kept when their line passes through
+    # them (pass 2 rejects them): the filter tests the line, not the half-line
+    behind_through = (b > 0) & (ww > 1.5 * r2) & (rho2 < 0.9 * r2)
+    assert behind_through.sum() > 100
+    assert keep[behind_through].all() and not hit[behind_through].any()
 
 
 # ---- cubes ---------------------------------------------------------------
