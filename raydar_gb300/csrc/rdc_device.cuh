@@ -374,9 +374,9 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 // LBVH's box test (rdc_bvh.cuh) on every cube of a chunk (up to 32, two per
 // packed instruction), into a bit mask of the cubes the exact pass 2
 // (cube_exact) has to decide.  A cube is dropped only when the grown box
-// [min - m, max + m] lies wholly behind the origin, is missed, or is entered
-// strictly beyond the best hit so far (the reference replaces only on a
-// strictly smaller t, and best only shrinks within the chunk).  The growth
+// [min - m, max + m] lies wholly behind the origin or is missed (dropping
+// boxes entered beyond the best hit too measured slower on cube-heavy
+// scenes: the extra candidates cost pass 2 less than the test cost here).  The growth
 // m = 2^-20 (|o| + 2R) + 1e-30, R >= |centre| + half side * sqrt(3) over the
 // run, covers the reference's slab rounding and this test's own (the bound
 // is proven for the LBVH's leaves, which run the same exact test after the
@@ -418,8 +418,7 @@ __device__ __forceinline__ CubeFilterRay cube_filter_ray(const RayPre& r, float 
 __device__ __forceinline__ float2 cube_planes(float2 p, float2 inv, float2 ns) { return fma2(p, inv, ns); }
 
 template <int Unroll>
-__device__ __forceinline__ uint32_t cube_candidates(const float4* __restrict__ pr, int n, const CubeFilterRay& c,
-                                                    float best) {
+__device__ __forceinline__ uint32_t cube_candidates(const float4* __restrict__ pr, int n, const CubeFilterRay& c) {
     const float2* p2 = reinterpret_cast<const float2*>(pr);
     const float2* nx = p2 + c.near_off[0];
     const float2* fx = p2 + (1 - c.near_off[0]);
@@ -427,7 +426,6 @@ __device__ __forceinline__ uint32_t cube_candidates(const float4* __restrict__ p
     const float2* fy = p2 + 2 + (1 - c.near_off[1]);
     const float2* nz = p2 + 4 + c.near_off[2];
     const float2* fz = p2 + 4 + (1 - c.near_off[2]);
-    const float2 b2 = f2(best, best);
     uint32_t m = 0;
     const int np = (n + 1) >> 1;
 #pragma unroll Unroll
@@ -439,10 +437,9 @@ __device__ __forceinline__ uint32_t cube_candidates(const float4* __restrict__ p
         const float2 entry = f2(fmax3(ex.x, ey.x, ez.x), fmax3(ex.y, ey.y, ez.y));
         const float2 exit = f2(fmin3(xx.x, xy.x, xz.x), fmin3(xx.y, xy.y, xz.y));
         const float2 span = sub2(exit, entry);  // exit >= entry
-        const float2 lead = sub2(b2, entry);    // entry <= best
-        // bit 31 set <=> dropped (exit < 0, exit < entry or entry > best)
-        const uint32_t w0 = __float_as_uint(span.x) | __float_as_uint(lead.x) | __float_as_uint(exit.x);
-        const uint32_t w1 = __float_as_uint(span.y) | __float_as_uint(lead.y) | __float_as_uint(exit.y);
+        // bit 31 set <=> dropped (exit < 0 or exit < entry)
+        const uint32_t w0 = __float_as_uint(span.x) | __float_as_uint(exit.x);
+        const uint32_t w1 = __float_as_uint(span.y) | __float_as_uint(exit.y);
         m = __funnelshift_l(~w0, m, 1);
         m = __funnelshift_l(~w1, m, 1);
     }
@@ -483,7 +480,7 @@ __device__ __forceinline__ void intersect_runs(const float4* __restrict__ rec,
                 for (int cb = run.y; cb < run.z; cb += 32) {
                     const int n = min(32, run.z - cb);
                     const float4* pr = pr0 + 3 * ((cb - run.y) >> 1);
-                    uint32_t m = cube_candidates<Unroll>(pr, n, c, best);
+                    uint32_t m = cube_candidates<Unroll>(pr, n, c);
                     while (m != 0u) {  // highest bit first = scene order
                         const int pos = 31 - __clz(m);
                         m ^= 1u << pos;

@@ -13,8 +13,7 @@ than three times its first-order rounding bound.  The reference's decision
 computes.  Inputs: rays grazing spheres just outside and inside their
 radius, rays leaving a sphere's surface (the self-intersection case whose
 roots straddle 0), far origins and centres, huge and tiny radii; rays aimed
-at cube edges and corners, starting on cube faces and inside cubes, with the
-best hit so far equal to and below the cube's own t."""
+at cube edges and corners, starting on cube faces and inside cubes."""
 import numpy as np
 
 F = np.float32
@@ -178,7 +177,7 @@ def _cube_run_bound(c, h):
     return np.nextafter(f, F(np.inf)) if float(f) < R else f
 
 
-def _cube_filter_keeps(o, d, lo, hi, R, best):
+def _cube_filter_keeps(o, d, lo, hi, R):
     """cube_filter_ray + cube_candidates (rdc_device.cuh), one cube per row."""
     inv = (F(1) / d).astype(F)
     ol1 = (np.abs(o[:, 0]) + np.abs(o[:, 1])) + np.abs(o[:, 2])
@@ -196,7 +195,7 @@ def _cube_filter_keeps(o, d, lo, hi, R, best):
     entry = e.max(axis=1)
     exit_ = x.min(axis=1)
     s = np.signbit
-    return ~(s(exit_ - entry) | s(best - entry) | s(exit_))
+    return ~(s(exit_ - entry) | s(exit_))
 
 
 def _cubes(rng, n, scale_c, h_lo, h_hi):
@@ -241,17 +240,8 @@ def test_cube_filter_never_drops_a_hit():
             t = _reference_cube_t(o, d, lo, hi)
             hit = ~np.isnan(t)
             R = _cube_run_bound(c, h)
-            keep = _cube_filter_keeps(o, d, lo, hi, R, np.full(len(c), np.inf, F))
+            keep = _cube_filter_keeps(o, d, lo, hi, R)
             assert not (hit & ~keep).any(), f"{mode}: a reference hit dropped"
-            # with best = the hit's own t (an equal t must still be kept) ...
-            keep_eq = _cube_filter_keeps(o, d, lo, hi, R, np.where(hit, t, F(np.inf)))
-            assert not (hit & ~keep_eq).any(), f"{mode}: a hit at t == best dropped"
-            # ... and best just below it drops most of them (the entry cut works)
-            below = np.where(hit, np.nextafter(t, F(-np.inf)), F(np.inf))
-            below = np.where(hit & (t > 0), below * F(0.5), below)
-            keep_below = _cube_filter_keeps(o, d, lo, hi, R, below)
-            if mode == "edge" and scale_c * 2.0 ** -18 < h_lo:  # growth well below the cube size
-                assert (hit & keep_below).sum() < 0.05 * hit.sum()
             n_hit += int(hit.sum())
     assert n_hit > 200_000
 
@@ -262,7 +252,7 @@ def test_cube_filter_culls_clear_misses():
     o = (c + _unit(rng.normal(size=(len(c), 3))) * (h * 4)[:, None]).astype(F)
     d = _unit(rng.normal(size=(len(c), 3))).astype(F)
     t = _reference_cube_t(o, d, lo, hi)
-    keep = _cube_filter_keeps(o, d, lo, hi, _cube_run_bound(c, h), np.full(len(c), np.inf, F))
+    keep = _cube_filter_keeps(o, d, lo, hi, _cube_run_bound(c, h))
     hit = ~np.isnan(t)
     assert not (hit & ~keep).any()
     # the box grown by about 2^-20 (|o| + 2R) keeps hardly anything the cube misses
