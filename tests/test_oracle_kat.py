@@ -165,3 +165,49 @@ def test_diffuse_is_flipped_into_the_hemisphere():
     o, d = oracle.scatter(sc, np.zeros((n, 3)), np.tile([0, 0, 1.0], (n, 1)), np.full(n, 4.0), np.zeros(n),
                           words)
     assert np.all(d @ np.array([0, 0, -1.0]) >= 0)
+
+
+def _glass_case(origin, direction, t, fresnel_word):
+    """One glass scatter (sphere r=1 at (0,0,5), ior 1.5, roughness 0) with
+    the transmission draw taken (word 6 = 0) and the given Fresnel word 7."""
+    sc = _scene([_sphere([0, 0, 5], 1.0, transmission=1.0, ior=1.5, roughness=0.0)]).to_c()
+    words = np.zeros((1, 12), np.uint32)
+    words[0, 7] = fresnel_word
+    o, d = oracle.scatter(sc, [origin], [direction], [t], [0], words)
+    return o[0].astype(np.float64), d[0].astype(np.float64)
+
+
+def test_glass_reflects_when_the_fresnel_draw_is_below_schlick():
+    # cpu.rs:284-304: hit from outside at (0, 0.6, 4.2), n = (0, 0.6, -0.8),
+    # cos_theta = 0.8; U_fresnel = 0 < R(theta) takes the specular direction
+    # reflect(d, n) = d - 2 (d.n) n = (0, 0.96, -0.28).  The ray still counts
+    # as a transmission ray: its origin is offset along the new direction.
+    o, d = _glass_case([0, 0.6, 0], [0, 0, 1], 4.2, 0)
+    assert np.allclose(d, [0.0, 0.96, -0.28], atol=2e-6)
+    assert np.allclose(o, np.array([0.0, 0.6, 4.2]) + 1e-4 * d, atol=2e-6)
+
+
+def test_glass_total_internal_reflection_from_inside():
+    # From inside, outgoing at (0, 0.9, 5 + sqrt(0.19)): back face, the normal
+    # flipped to face the ray, ratio = ior = 1.5, sin_theta = 0.9 and
+    # 1.5 * 0.9 > 1: can_refract fails (utils/mod.rs:37-44) even though the
+    # Fresnel draw (~1) exceeds R(theta), so the direction is the reflection.
+    z = 5.0 + np.sqrt(0.19)
+    o, d = _glass_case([0, 0.9, 5.0], [0, 0, 1], z - 5.0, 0xFFFFFFFF)
+    n = np.array([0.0, -0.9, -np.sqrt(0.19)])  # the face normal seen by the ray
+    want = np.array([0.0, 0.0, 1.0]) - 2 * n[2] * n
+    assert np.allclose(d, want, atol=2e-6)
+    assert d[2] > 0 and d[1] < 0  # reflected back into the sphere's interior half-space
+
+
+def test_glass_refraction_obeys_snell_at_oblique_incidence():
+    # Same hit as the Fresnel case with U_fresnel ~ 1: refract with ratio
+    # 1/1.5 (utils/mod.rs:25-35): perp = (0, 0.32, 0.24), parallel =
+    # -sqrt(1 - 0.16) n, so the refracted direction makes sin = 0.6 / 1.5 = 0.4
+    # with the inward normal.
+    o, d = _glass_case([0, 0.6, 0], [0, 0, 1], 4.2, 0xFFFFFFFF)
+    n = np.array([0.0, 0.6, -0.8])
+    want = np.array([0.0, 0.32, 0.24]) - np.sqrt(1 - 0.16) * n
+    assert np.allclose(d, want, atol=2e-6)
+    sin_t = np.linalg.norm(np.cross(d, -n))
+    assert abs(sin_t - 0.4) < 2e-6
