@@ -211,3 +211,27 @@ def test_glass_refraction_obeys_snell_at_oblique_incidence():
     assert np.allclose(d, want, atol=2e-6)
     sin_t = np.linalg.norm(np.cross(d, -n))
     assert abs(sin_t - 0.4) < 2e-6
+
+
+def test_metal_lobe_adds_the_unit_sphere_sample_scaled_by_roughness_squared():
+    # cpu.rs:262-279: specular = normalize(reflect(d, n) + s * roughness^2),
+    # s = normalize(U[-1,1]^3) (utils/mod.rs:47-55).  All-ones words give
+    # gen_range values of 1 - 2^-22 each (rand 0.8.5), so s = (1,1,1)/sqrt(3).
+    sc = _scene([_sphere([0, 0, 5], 1.0, metallic=1.0, roughness=0.5)]).to_c()
+    words = np.full((1, 12), 0xFFFFFFFF, np.uint32)
+    words[0, 7] = 0  # U_metal = 0 < 1: the specular lobe
+    o, d = oracle.scatter(sc, [[0, 0, 0]], [[0, 0, 1]], [4.0], [0], words)
+    v = np.array([0.0, 0.0, -1.0]) + 0.25 * np.ones(3) / np.sqrt(3.0)
+    assert np.allclose(d[0], v / np.linalg.norm(v), atol=2e-6)
+
+
+def test_cube_edge_hit_takes_the_y_face():
+    # cpu.rs:354-394: the face is chosen by strict comparisons of the distances
+    # to the three slab pairs, x first: on the edge x = y = 1 both distances are
+    # 0, x < y fails, y < z holds, so the normal is +y (and the ray, coming down
+    # the diagonal, sees it as a front face).
+    sc = _scene([_cube([0, 0, 0], 2.0)]).to_c()
+    t, idx, nrm, fr = oracle.intersect(sc, np.array([[2.0, 2.0, 0.0]], np.float32),
+                                       np.array([[-1.0, -1.0, 0.0]], np.float32))
+    assert idx[0] == 0 and t[0] == 1.0
+    assert nrm[0].tolist() == [0.0, 1.0, 0.0] and fr[0] == 1
