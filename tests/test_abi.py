@@ -25,6 +25,14 @@ def test_every_declared_symbol_is_exported_and_bound():
     assert set(native.SIGNATURES) == set(names)
 
 
+def test_the_rust_binding_declares_every_entry_point():
+    """INTEGRATION.md's extern block (the FFI a maintainer adds on the Rust
+    side) names every function the header declares, and nothing else."""
+    text = (ROOT / "INTEGRATION.md").read_text()
+    bound = set(re.findall(r"pub fn (rdc_[a-z0-9_]+)\(", text))
+    assert bound == set(_declared())
+
+
 def test_version_string():
     assert b"sm_103a" in native.load().rdc_version()
 
