@@ -233,11 +233,18 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count,
  * up the array's device address; make it before any stream capture.  Every
  * call on a device shares the array: calls that overlap on the GPU race and
  * must be serialised by the caller.  If `segments_out` is non-NULL the call
- * waits for the render and stores its segment count.  A message for a
- * non-OK status is written to `error_out` (capacity bytes, may be NULL).
+ * waits for the render, stores its segment count and reports a device error
+ * (a block that could not stage the scene into shared memory) as
+ * RDC_ERR_DEVICE; with segments_out NULL it returns once the work is queued
+ * and device errors are not reported, so pass it wherever they must be
+ * checked.  A message for a non-OK status is written to `error_out`
+ * (capacity bytes, may be NULL).
  * No counterpart in the reference: it has no allocation-free entry point. */
 #define RDC_STATIC_MAX_OBJECTS 1024u
-#define RDC_STATIC_SCRATCH_BYTES 131328u /* 256 B counters + 128 B per object slot */
+/* 256 B of counters + 160 B per object slot: up to 4 intersection records
+ * of 16 B (a one-cube run takes 4), 16 B of hit data, a 64 B material and a
+ * 16 B run entry. */
+#define RDC_STATIC_SCRATCH_BYTES 164096u
 rdc_status rdc_render_static(const rdc_scene_desc* scene, float* accum_device, uint32_t spp_begin,
                              uint32_t spp_count, uint32_t max_bounces, uint64_t seed, void* stream,
                              uint64_t* segments_out, char* error_out, size_t error_capacity);

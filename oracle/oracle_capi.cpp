@@ -178,7 +178,7 @@ void oracle_tonemap(const float* accum, uint32_t npix, uint32_t sample_count, ui
     for (size_t i = 0; i < (size_t)npix * 4; ++i) out[i] = tonemap_channel(accum[i], sample_count);
 }
 
-// Camera::update_matrices in float, inverses evaluated in double.
+// Camera::update_matrices in float, including cgmath's float inverse.
 int oracle_camera_matrices(const rdc_camera* c, float view[16], float proj[16], float inv_view[16],
                            float inv_proj[16]) {
     const V3<float> eye = v3(c->position[0], c->position[1], c->position[2]);
@@ -192,13 +192,8 @@ int oracle_camera_matrices(const rdc_camera* c, float view[16], float proj[16], 
         const float sz = c->ortho_size;
         ortho(-sz * aspect, sz * aspect, -sz, sz, c->near_clip, c->far_clip, proj);
     }
-    double a[16], b[16];
-    for (int i = 0; i < 16; ++i) a[i] = view[i];
-    if (!invert4(a, b)) return 1;
-    for (int i = 0; i < 16; ++i) inv_view[i] = (float)b[i];
-    for (int i = 0; i < 16; ++i) a[i] = proj[i];
-    if (!invert4(a, b)) return 1;
-    for (int i = 0; i < 16; ++i) inv_proj[i] = (float)b[i];
+    if (!invert4_cgmath(view, inv_view)) return 1;
+    if (!invert4_cgmath(proj, inv_proj)) return 1;
     return 0;
 }
 

@@ -33,8 +33,9 @@
 // (slot 6), then U_fresnel or U_metallic (slot 7), then s3 (slots 8-10) or
 // U_roughness (slot 8).
 //
-// PARITY STATUS: camera matrices are pinned against the matrices the
-// reference serialised into scenes/default.rscn and scenes/benchmark.rscn.
+// PARITY STATUS: camera matrices (view, projection and both inverses, bit
+// for bit) are pinned against the matrices the reference serialised into
+// scenes/default.rscn and scenes/benchmark.rscn.
 // The rest of the path is pinned only by hand-derived known answers: the
 // reference has no tests, no fixtures and cannot be built here (no Rust
 // toolchain), so per-path arithmetic is "parity unpinned" against the
@@ -566,36 +567,60 @@ static inline void ortho(T l, T r, T b, T t, T n, T f, T m[16]) {
     m[15] = T(1);
 }
 
-// General 4x4 inverse by cofactors, evaluated in double.
-static inline bool invert4(const double a[16], double out[16]) {
-    // a is column-major; work with r[row][col].
-    double r[4][4];
-    for (int c = 0; c < 4; ++c)
-        for (int w = 0; w < 4; ++w) r[w][c] = a[c * 4 + w];
-    double inv[4][4];
-    double det = 0.0;
+// cgmath 0.18.0 Matrix3::determinant for a matrix given as m[col][row]:
+// m00 (m11 m22 - m21 m12) - m10 (m01 m22 - m21 m02) + m20 (m01 m12 - m11 m02),
+// evaluated left to right in float.
+static inline float det3(const float m[3][3]) {
+    return m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) - m[1][0] * (m[0][1] * m[2][2] - m[2][1] * m[0][2]) +
+           m[2][0] * (m[0][1] * m[1][2] - m[1][1] * m[0][2]);
+}
+
+// cgmath 0.18.0 Matrix4::invert in float (the reference's call at
+// src/scene/camera.rs:229-230).  a is column-major, a[c*4+r].
+//   determinant: Laplace expansion along row 0, a00 d0 - a10 d1 + a20 d2 - a30 d3,
+//     where d_k is the Matrix3::new(...) of rows 1..3 without column k, built
+//     column by column from the ORIGINAL ROWS (so it is the transposed minor).
+//   singular when |det| <= f32::EPSILON (approx's ulps_eq! against zero; the
+//     reference then unwraps None and panics).
+//   entry (column i, row j) = det3(minor) * sign * (1 / det), the minor being
+//     Matrix3::from_cols of the transpose's rows != i, each truncated at j,
+//     sign = -1 when i + j is odd.
+static inline bool invert4_cgmath(const float a[16], float out[16]) {
+    auto at = [&](int c, int r) { return a[c * 4 + r]; };
+    float d[4];
+    for (int k = 0; k < 4; ++k) {
+        float m[3][3];
+        int mc = 0;
+        for (int c = 0; c < 4; ++c) {
+            if (c == k) continue;
+            // Matrix3::new(c0r0, c0r1, c0r2, ...) with c0 = (a[1][c], ...) over the kept columns
+            m[0][mc] = at(c, 1);
+            m[1][mc] = at(c, 2);
+            m[2][mc] = at(c, 3);
+            ++mc;
+        }
+        d[k] = det3(m);
+    }
+    const float det = at(0, 0) * d[0] - at(1, 0) * d[1] + at(2, 0) * d[2] - at(3, 0) * d[3];
+    if (!(std::fabs(det) > 1.1920929e-7f)) return false;  // also NaN
+    const float inv_det = 1.0f / det;
     for (int i = 0; i < 4; ++i) {
         for (int j = 0; j < 4; ++j) {
-            double m[3][3];
-            for (int p = 0, mi = 0; p < 4; ++p) {
-                if (p == i) continue;
-                for (int q = 0, mj = 0; q < 4; ++q) {
-                    if (q == j) continue;
-                    m[mi][mj++] = r[p][q];
+            float m[3][3];
+            int mc = 0;
+            for (int rr = 0; rr < 4; ++rr) {  // transpose's vector rr = row rr of a
+                if (rr == i) continue;
+                int mr = 0;
+                for (int cc = 0; cc < 4; ++cc) {
+                    if (cc == j) continue;
+                    m[mc][mr++] = at(cc, rr);
                 }
-                ++mi;
+                ++mc;
             }
-            const double minor = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
-                                 m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
-                                 m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
-            const double cof = ((i + j) & 1) ? -minor : minor;
-            inv[j][i] = cof;  // adjugate = transpose of cofactors
-            if (i == 0) det += r[0][j] * cof;
+            const float sign = ((i + j) & 1) ? -1.0f : 1.0f;
+            out[i * 4 + j] = det3(m) * sign * inv_det;
         }
     }
-    if (det == 0.0 || det != det) return false;
-    for (int c = 0; c < 4; ++c)
-        for (int w = 0; w < 4; ++w) out[c * 4 + w] = inv[w][c] / det;
     return true;
 }
 

@@ -96,7 +96,7 @@ def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure) with -ffp-contract=off."""
     (ORACLE_DIR / "_build").mkdir(exist_ok=True)
     deps = [ORACLE_DIR / "oracle_capi.cpp", ORACLE_DIR / "raydar_oracle.hpp", ORACLE_DIR / "raydar_oracle_grad.hpp",
-            INCLUDE / "raydar_cuda.h"]
+            ORACLE_DIR / "Makefile", INCLUDE / "raydar_cuda.h"]
     if force or _stale(ORACLE_LIB, deps):
         _run(["make", "-s", "-C", str(ORACLE_DIR)])
     return ORACLE_LIB

@@ -3,11 +3,10 @@
 // look_at_lh(position, target, up), proj = GL-style perspective or ortho,
 // and both inverses.  Host code only; compiled with -ffp-contract=off.
 //
-// The view and projection entries are evaluated in float with cgmath 0.18's
-// published formulas.  The inverses are computed in double by Gauss-Jordan
-// elimination with partial pivoting and rounded once to float; the
-// reference's own float inversion differs from that by at most a few ulp
-// (the tests pin both against the matrices stored in the reference scenes).
+// Every entry is evaluated in float with the published formulas of cgmath
+// 0.18.0 (the version the reference pins), in their order of operations, so
+// the four matrices equal the reference's bit for bit (the tests pin them
+// against the matrices stored in the reference's own scene files).
 #include <cmath>
 #include <cstring>
 
@@ -29,31 +28,59 @@ F3 f3cross(F3 a, F3 b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 
-// Inverse of a column-major 4x4 matrix; false if singular.
-bool invert_gauss_jordan(const float in[16], float out[16]) {
-    double m[4][8];
-    for (int r = 0; r < 4; ++r) {
-        for (int c = 0; c < 4; ++c) m[r][c] = in[c * 4 + r];
-        for (int c = 0; c < 4; ++c) m[r][4 + c] = (r == c) ? 1.0 : 0.0;
+// 3x3 determinant of m (m[col][row]) expanded along its first row, as
+// cgmath's Matrix3::determinant groups it:
+// m00 (m11 m22 - m21 m12) - m10 (m01 m22 - m21 m02) + m20 (m01 m12 - m11 m02).
+float det3(const float m[3][3]) {
+    const float t0 = m[1][1] * m[2][2] - m[2][1] * m[1][2];
+    const float t1 = m[0][1] * m[2][2] - m[2][1] * m[0][2];
+    const float t2 = m[0][1] * m[1][2] - m[1][1] * m[0][2];
+    return m[0][0] * t0 - m[1][0] * t1 + m[2][0] * t2;
+}
+
+// 3x3 matrix whose column k is row rows[k] of the column-major 4x4 `a`
+// restricted to the columns cols[0..2] (a minor, laid out transposed).
+void minor_by_rows(const float a[16], const int rows[3], const int cols[3], float m[3][3]) {
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) m[k][l] = a[cols[l] * 4 + rows[k]];
+}
+
+// The three indices of 0..3 other than `skip`, ascending.
+void others(int skip, int out[3]) {
+    for (int i = 0, n = 0; i < 4; ++i)
+        if (i != skip) out[n++] = i;
+}
+
+// Inverse of a column-major 4x4 matrix by cofactors, as cgmath 0.18.0's
+// Matrix4::invert computes it in float: det by expansion along row 0 with
+// transposed minors of rows 1..3, singular when |det| <= f32::EPSILON (its
+// ulps_eq! test against zero), then entry (column i, row j) =
+// det3(minor without row i and column j, transposed) * (+-1) * (1 / det).
+bool invert_cgmath(const float a[16], float out[16]) {
+    static const int kRows123[3] = {1, 2, 3};
+    float dk[4];
+    for (int k = 0; k < 4; ++k) {
+        int cols[3];
+        others(k, cols);
+        float m[3][3];
+        minor_by_rows(a, kRows123, cols, m);
+        dk[k] = det3(m);
     }
-    for (int col = 0; col < 4; ++col) {
-        int piv = col;
-        for (int r = col + 1; r < 4; ++r)
-            if (std::fabs(m[r][col]) > std::fabs(m[piv][col])) piv = r;
-        if (m[piv][col] == 0.0 || !std::isfinite(m[piv][col])) return false;
-        if (piv != col)
-            for (int c = 0; c < 8; ++c) std::swap(m[piv][c], m[col][c]);
-        const double p = m[col][col];
-        for (int c = 0; c < 8; ++c) m[col][c] /= p;
-        for (int r = 0; r < 4; ++r) {
-            if (r == col) continue;
-            const double f = m[r][col];
-            if (f == 0.0) continue;
-            for (int c = 0; c < 8; ++c) m[r][c] -= f * m[col][c];
+    const float det = a[0] * dk[0] - a[4] * dk[1] + a[8] * dk[2] - a[12] * dk[3];
+    if (!(std::fabs(det) > 1.1920929e-7f)) return false;  // singular or NaN: the reference unwraps None
+    const float inv_det = 1.0f / det;
+    for (int i = 0; i < 4; ++i) {
+        int rows[3];
+        others(i, rows);
+        for (int j = 0; j < 4; ++j) {
+            int cols[3];
+            others(j, cols);
+            float m[3][3];
+            minor_by_rows(a, rows, cols, m);
+            const float sign = ((i + j) & 1) ? -1.0f : 1.0f;
+            out[i * 4 + j] = det3(m) * sign * inv_det;
         }
     }
-    for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) out[c * 4 + r] = (float)m[r][4 + c];
     return true;
 }
 
@@ -105,7 +132,7 @@ extern "C" rdc_status rdc_camera_update_matrices(rdc_camera* cam) {
     }
     // The reference unwraps the inverses (camera.rs:229-230); a singular
     // matrix is reported here instead of panicking.
-    if (!invert_gauss_jordan(cam->view_matrix, cam->inverse_view_matrix)) return RDC_ERR_INVALID_ARGUMENT;
-    if (!invert_gauss_jordan(cam->proj_matrix, cam->inverse_proj_matrix)) return RDC_ERR_INVALID_ARGUMENT;
+    if (!invert_cgmath(cam->view_matrix, cam->inverse_view_matrix)) return RDC_ERR_INVALID_ARGUMENT;
+    if (!invert_cgmath(cam->proj_matrix, cam->inverse_proj_matrix)) return RDC_ERR_INVALID_ARGUMENT;
     return RDC_OK;
 }

@@ -28,7 +28,19 @@
 namespace {
 
 constexpr size_t kCounterBytes = 256;
-constexpr size_t kRecBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 32;  // <= 2 float4 per object
+// Intersection records per object, worst case: a run of L objects takes
+// 3 * ceil(L / 2) float4 (spheres) or 1 + 3 * ceil(L / 2) (cubes, with the
+// run header), at most 4 per object, reached by a one-cube run.  A scene of
+// alternating spheres and cubes takes 3.5 per object.
+constexpr size_t kRecPerObject = 4;
+constexpr size_t kMaxRec = (size_t)RDC_STATIC_MAX_OBJECTS * kRecPerObject;
+constexpr size_t kRecBytes = kMaxRec * 16;
+constexpr bool run_records_fit(uint32_t max_len) {
+    for (uint32_t len = 1; len <= max_len; ++len)
+        if (1u + 3u * ((len + 1u) / 2u) > kRecPerObject * len) return false;
+    return true;
+}
+static_assert(run_records_fit(RDC_STATIC_MAX_OBJECTS), "a run can take more records than the scratch allows");
 constexpr size_t kHitBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 16;
 constexpr size_t kMatBytes = (size_t)RDC_STATIC_MAX_OBJECTS * sizeof(rdc::MatDev);
 constexpr size_t kRunBytes = (size_t)RDC_STATIC_MAX_OBJECTS * 16;
@@ -82,7 +94,7 @@ rdc_status setup(int device, unsigned char** scratch, int* sms, char* err, size_
 // Host staging for the flattened scene: static storage (no allocation),
 // guarded by a mutex while a call flattens and copies it.
 std::mutex g_stage_mutex;
-float4 g_stage_rec[2 * RDC_STATIC_MAX_OBJECTS];
+float4 g_stage_rec[kMaxRec];
 float4 g_stage_hit[RDC_STATIC_MAX_OBJECTS];
 rdc::MatDev g_stage_mat[RDC_STATIC_MAX_OBJECTS];
 int4 g_stage_runs[RDC_STATIC_MAX_OBJECTS];
@@ -165,6 +177,12 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
     // (pageable copies are staged before cudaMemcpyAsync returns).
     const uint32_t n = sc->object_count;
     const rdc::FlatCounts fc = rdc::flat_counts(sc);
+    // Never above the regions by the worst case above; checked all the same,
+    // before anything is written to the staging arrays or the scratch.
+    if (fc.nrec > kMaxRec || fc.nruns > RDC_STATIC_MAX_OBJECTS) {
+        set_error(error_out, error_capacity, "rdc_render_static: flattened scene exceeds the fixed scratch");
+        return RDC_ERR_LIMIT;
+    }
     bool fast_div = true;
     {
         std::lock_guard<std::mutex> lock(g_stage_mutex);

@@ -13,6 +13,7 @@ the library's rdc_camera_update_matrices (src/scene/camera.rs:210-231).
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import json
 from dataclasses import dataclass, field
@@ -24,6 +25,25 @@ import numpy as np
 from . import native
 
 f32 = np.float32
+
+# Camera::update_matrices goes through the library unless a caller routes it
+# elsewhere with `camera_matrices_from` (a function of an RdcCamera returning
+# the view, projection and both inverse matrices as 16 column-major floats).
+_matrices_fn = None
+
+
+@contextlib.contextmanager
+def camera_matrices_from(fn):
+    """Within the block, compute camera matrices with `fn(RdcCamera) ->
+    (view, proj, inverse_view, inverse_proj)` instead of the library's
+    rdc_camera_update_matrices: lets a process that must not load the CUDA
+    library (a CPU-only timing of the same scene) build scenes."""
+    global _matrices_fn
+    prev, _matrices_fn = _matrices_fn, fn
+    try:
+        yield
+    finally:
+        _matrices_fn = prev
 
 
 def _v3(d) -> np.ndarray:
@@ -100,9 +120,14 @@ class Camera:
         return c
 
     def update_matrices(self) -> None:
-        """Camera::update_matrices (camera.rs:210-231) via the native library."""
-        lib = native.load()
+        """Camera::update_matrices (camera.rs:210-231) via the native library
+        (or the function installed by `camera_matrices_from`)."""
         c = self.to_c()
+        if _matrices_fn is not None:
+            mats = [np.asarray(m, np.float32).reshape(16).copy() for m in _matrices_fn(c)]
+            self.view_matrix, self.proj_matrix, self.inverse_view_matrix, self.inverse_proj_matrix = mats
+            return
+        lib = native.load()
         st = lib.rdc_camera_update_matrices(C.byref(c))
         if st != native.RDC_OK:
             raise native.RdcError(st, "rdc_camera_update_matrices: singular or invalid camera")

@@ -148,3 +148,33 @@ def test_range_guards_turn_the_fast_path_off(probe):
     scene.objects[2].size = 0.0  # a cube side must be > 0
     _, _, fast = _flatten(probe, scene)
     assert not fast
+
+
+def _header_define(name):
+    import re
+    txt = (build.INCLUDE / "raydar_cuda.h").read_text()
+    return int(re.search(rf"#define {name} (\d+)u", txt).group(1))
+
+
+def test_worst_case_layout_fits_the_static_scratch(probe):
+    """rdc_render_static keeps the flattened scene in a fixed device array.
+    Its record region must hold the layout of any scene of up to
+    RDC_STATIC_MAX_OBJECTS objects: alternating spheres and cubes (every run
+    of length one: 3 records per sphere, 4 per cube with the run header) is
+    the densest, 3584 records for 1024 objects."""
+    nmax = _header_define("RDC_STATIC_MAX_OBJECTS")
+    scratch = _header_define("RDC_STATIC_SCRATCH_BYTES")
+    # counters 256 B; per object slot: hit 16 B, material 64 B, run 16 B; the rest is records
+    rec_capacity = (scratch - 256 - nmax * (16 + 64 + 16)) // 16
+    rng = np.random.default_rng(77)
+    for kinds in ("SC" * (nmax // 2), "CS" * (nmax // 2), "C" + "SC" * ((nmax - 1) // 2)):
+        rec, runs, _ = _flatten(probe, _scene(rng, kinds))
+        assert len(runs) == len(kinds)
+        assert len(rec) == sum(3 if k == "S" else 4 for k in kinds)
+        assert len(rec) <= rec_capacity, (len(rec), rec_capacity)
+    # any mix: never more than 4 records per object
+    for _ in range(20):
+        n = int(rng.integers(1, nmax + 1))
+        kinds = "".join(rng.choice(["S", "C"], n, p=[0.5, 0.5]))
+        rec, _, _ = _flatten(probe, _scene(rng, kinds))
+        assert len(rec) <= 4 * n <= rec_capacity
