@@ -450,8 +450,9 @@ def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
     adj = float((ge[j] * np.asarray(scene.objects[j].material.emission_color, np.float32)).sum())
     checks.append({"param": f"emission_strength[{j}]", "adjoint": adj, "central_difference": fd,
                    "rel_gap": abs(fd - adj) / max(abs(fd), 1e-30)})
-    # roughness: the difference quotient also holds the paths whose hit or lobe
-    # flips within the step, which path replay leaves out (a stated gap)
+    # roughness on this cluttered scene: the difference quotient also holds the
+    # paths whose hit object changes within the step (silhouette crossings, a
+    # boundary term the estimator leaves out), so this entry states the gap
     metals = [i for i, o in enumerate(scene.objects) if o.material.metallic == 1.0 and o.material.roughness > 0.1]
     j = max(metals, key=lambda i: abs(gr[i]))
     lo, hi = copy.deepcopy(scene), copy.deepcopy(scene)
@@ -462,8 +463,9 @@ def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
     fd = float((loss(hi) - loss(lo)) / den)
     checks.append({"param": f"roughness[{j}]", "adjoint": float(gr[j]), "central_difference": fd,
                    "rel_gap": abs(fd - float(gr[j])) / max(abs(fd), 1e-30),
-                   "note": "difference includes hit/lobe changes that path replay omits"})
+                   "note": "c4 scene: the difference includes silhouette crossings the estimator omits"})
     r.close()
+    rough_checks = roughness_fd_checks(local)
     f_ms, b_ms = sum(fwd_ms) / steps, sum(bwd_ms) / steps
     return {
         "workload": "c4_diff: 512x512, 128 spp, 6 bounces, 32 spheres + 2 emissive + ground; L2 loss to a "
@@ -473,7 +475,44 @@ def adjoint_bench(local: int, steps: int, fd_spp: int = 4096):
         "backward_replayed_segments_per_s": bwd_segs / (sum(bwd_ms) / 1e3),
         "steps": steps, "wall_s": wall,
         "fd_check": {"spp": fd_spp, "eps": 1e-3, "common_random_numbers": True, "params": checks},
+        "roughness_fd_check": rough_checks,
     }
+
+
+def roughness_fd_checks(local: int, eps: float = 1e-2):
+    """The roughness gradient against central differences (common random
+    numbers) on the three scenes where they are well defined
+    (tests/roughness_scenes.py): a lone rough metal sphere (pathwise part), a
+    lone Specular-class sphere (+ the diffuse/specular coin) and a rough metal
+    sphere over a glass floor (+ the Fresnel coin)."""
+    import copy
+
+    import numpy as np
+
+    from raydar_gb300 import CudaRenderer, RendererConfig
+    from tests import roughness_scenes as RS
+
+    out = []
+    for name, size, spp in (("lone_metal", 96, 256), ("lone_specular", 512, 4096), ("glass_floor", 512, 4096)):
+        scene, j, bounces = getattr(RS, name)(size)
+        dl = RS.pixel_weights(name, scene)
+        r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=1, device=local)
+        r.forward(scene, spp)
+        _, gr, _ = r.backward(scene, dl)
+
+        def loss(rho):
+            s = copy.deepcopy(scene)
+            s.objects[j].material.roughness = rho
+            return float((r.forward(s, spp).astype(np.float64) * dl).sum())
+
+        r0 = scene.objects[j].material.roughness
+        lo, hi = float(np.float32(r0 - eps)), float(np.float32(r0 + eps))
+        fd = (loss(hi) - loss(lo)) / (hi - lo)
+        r.close()
+        out.append({"scene": name, "size": size, "spp": spp, "eps": eps, "roughness": r0,
+                    "adjoint": float(gr[j]), "central_difference": fd,
+                    "rel_gap": abs(fd - float(gr[j])) / max(abs(fd), 1e-30)})
+    return out
 
 
 def reference_scene_bench(local: int, steps: int, spp: int = 16, bounces: int = 12):

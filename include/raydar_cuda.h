@@ -340,9 +340,15 @@ rdc_status rdc_forward(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uin
  * (NULL to skip): grad_albedo (N*3), grad_roughness (N, w.r.t.
  * Material::roughness), grad_emission (N*3, w.r.t. the emitted radiance
  * emission_color * emission_strength).  Each path is replayed from its
- * random-number counter; nothing from the forward pass is stored.  Discrete
- * events (which object a ray hits, which lobe a scatter takes) are held
- * fixed: roughness moves the gradient only through scatter directions. */
+ * random-number counter; nothing from the forward pass is stored.  The
+ * roughness gradient has a pathwise part (roughness bends scatter directions)
+ * and a lobe-choice part: where a coin whose probability depends on the
+ * parameters picked the lobe -- U < roughness^2 for diffuse over specular
+ * (src/renderer/cpu.rs:309), Schlick's reflectance for reflection over
+ * refraction (cpu.rs:296-297) -- the path adds the radiance it gathers after
+ * that choice times d log P (a score-function term, unbiased for
+ * 0 < roughness < 1).  Not included: changes of which object a ray hits
+ * (silhouette crossings) and the total-internal-reflection edge. */
 rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo, float* grad_roughness,
                         float* grad_emission);
 

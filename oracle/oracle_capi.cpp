@@ -70,7 +70,7 @@ int oracle_render(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t 
 // (may be null): paths whose double evaluation lost a recorded hit.
 int oracle_gradient(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed,
                     uint32_t stream, const float* dl_dimage, double* g_albedo, double* g_rough,
-                    double* g_emission, double* image, int threads, uint64_t* lost_out) {
+                    double* g_emission, double* image, int threads, uint64_t* lost_out, double* g_rough_path) {
     if (!desc || !dl_dimage || !g_albedo || !g_rough || !g_emission || n == 0) return 1;
     if (max_bounces > (uint32_t)kGradSlots) return 2;
     const Scene<float> sf = scene_from_desc<float>(desc);
@@ -79,18 +79,19 @@ int oracle_gradient(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_
     const uint32_t npix = s.width * s.height;
     const size_t nobj = s.objects.size();
     if (threads < 1) threads = 1;
-    std::vector<std::vector<double>> part(threads, std::vector<double>(7 * nobj, 0.0));
+    std::vector<std::vector<double>> part(threads, std::vector<double>(8 * nobj, 0.0));
     std::atomic<uint32_t> next{0};
     auto worker = [&](int tid) {
         double* ga = part[tid].data();
         double* gr = ga + 3 * nobj;
         double* ge = gr + nobj;
+        double* gp = ge + 3 * nobj;
         for (;;) {
             const uint32_t base = next.fetch_add(16);
             if (base >= npix) break;
             const uint32_t end = base + 16 < npix ? base + 16 : npix;
             lost += gradient_pixels(sf, s, base, end, s0, n, max_bounces, seed, stream, dl_dimage, ga, gr, ge,
-                                    image);
+                                    image, gp);
         }
     };
     if (threads == 1) {
@@ -106,12 +107,14 @@ int oracle_gradient(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_
             g_emission[3 * j + c] = 0.0;
         }
         g_rough[j] = 0.0;
+        if (g_rough_path) g_rough_path[j] = 0.0;
         for (int t = 0; t < threads; ++t) {
             for (int c = 0; c < 3; ++c) {
                 g_albedo[3 * j + c] += part[t][3 * j + c];
                 g_emission[3 * j + c] += part[t][4 * nobj + 3 * j + c];
             }
             g_rough[j] += part[t][3 * nobj + j];
+            if (g_rough_path) g_rough_path[j] += part[t][7 * nobj + j];
         }
     }
     if (lost_out) *lost_out = lost.load();

@@ -383,21 +383,28 @@ static inline V3<T> world_sample(const Scene<T>& s, V3<T> d) {
 }
 
 // The discrete choices of one scatter: which lobe, the diffuse flip, the
-// transmission branch and the |dir|^2 < 1e-10 fallback.  The gradient oracle
-// records them on the float path and replays that path in double with them
-// held fixed (the same estimator, evaluated at higher precision).
+// transmission branch and the |dir|^2 < 1e-10 fallback, and which coin with
+// a parameter-dependent probability decided the lobe: the roughness coin
+// (U_rough < roughness^2, cpu.rs:309) or the Fresnel coin (Schlick's R <
+// U_fresnel where refraction is possible, cpu.rs:296-297).  The gradient
+// oracle records them on the float path and replays that path in double with
+// them held fixed (the same estimator, evaluated at higher precision).
 enum { kLobeDiffuse = 0, kLobeSpecular = 1, kLobeRefract = 2 };
 struct Choice {
     int lobe;
     bool flip, trans, to_normal;
+    bool rough_coin, fresnel_coin;
 };
 
 // The hit branch of per_pixel, src/renderer/cpu.rs:262-333, given the
 // bounce's random words.  Updates the ray.  ch: if force, the choices to
-// take; else, when not null, receives the choices taken.
+// take; else, when not null, receives the choices taken.  coin_p, when not
+// null, receives the probability of the outcome the deciding coin gave
+// (T(1) when no such coin decided).
 template <typename T>
 static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& ob,
-                           const uint32_t* w, Ray<T>* out, Choice* ch = nullptr, bool force = false) {
+                           const uint32_t* w, Ray<T>* out, Choice* ch = nullptr, bool force = false,
+                           T* coin_p = nullptr) {
     const T roughness = ob.roughness * ob.roughness;
     const T metallic = ob.metallic;
     const T transmission = ob.transmission;
@@ -413,6 +420,8 @@ static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& 
     const bool transmission_ray = force ? ch->trans : (T)uniform01(w[6]) < transmission;
     V3<T> direction;
     int lobe = kLobeSpecular;
+    bool rough_coin = false, fresnel_coin = false;
+    T p_coin = T(1);
     if (transmission_ray) {
         T ior = ob.ior;
         if (h.front) ior = T(1) / ior;
@@ -424,8 +433,16 @@ static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& 
         const T m2 = m * m;
         const T m5 = m * (m2 * m2);                  // powi(5), square-and-multiply
         const T refl = r0 + (T(1) - r0) * m5;
-        const bool refr = force ? ch->lobe == kLobeRefract
-                                : (refl < (T)uniform01(w[7]) && can_refract(rd, h.normal, ior));
+        bool refr;
+        if (force) {
+            refr = ch->lobe == kLobeRefract;
+            fresnel_coin = ch->fresnel_coin;
+        } else {
+            const bool can = can_refract(rd, h.normal, ior);
+            refr = refl < (T)uniform01(w[7]) && can;
+            fresnel_coin = can;  // under total internal reflection the coin decides nothing
+        }
+        if (fresnel_coin) p_coin = refr ? T(1) - refl : refl;
         if (refr) {
             const V3<T> refracted = refract(rd, h.normal, ior);
             const V3<T> offset3 = mul(random_in_unit_sphere<T>(w + 8), roughness);
@@ -438,11 +455,14 @@ static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& 
                      : (T)uniform01(w[7]) < metallic) {
         direction = specular;
     } else {
+        rough_coin = true;
         if (force ? ch->lobe == kLobeDiffuse : (T)uniform01(w[8]) < roughness) {
             direction = diffuse;
             lobe = kLobeDiffuse;
+            p_coin = roughness;
         } else {
             direction = specular;
+            p_coin = T(1) - roughness;
         }
     }
     const V3<T> off = transmission_ray ? direction : h.normal;
@@ -450,7 +470,8 @@ static inline void scatter(const Ray<T>& ray, const Hit<T>& h, const Object<T>& 
     out->direction = direction;
     const bool to_normal = force ? ch->to_normal : magnitude2(out->direction) < T(1e-10f);
     if (to_normal) out->direction = h.normal;
-    if (ch && !force) *ch = Choice{lobe, flip, transmission_ray, to_normal};
+    if (ch && !force) *ch = Choice{lobe, flip, transmission_ray, to_normal, rough_coin, fresnel_coin};
+    if (coin_p) *coin_p = p_coin;
 }
 
 // Primary ray of pixel (x, y): src/renderer/cpu.rs:199-202, 234-251.

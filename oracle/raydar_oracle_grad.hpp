@@ -10,13 +10,22 @@
 //     dL/dE(j) = number of hits on j;
 //   - albedo: dL_c/dalbedo_c(j) = sky_c * sum over hits k on j of the product
 //     of the other hits' albedos;
-//   - roughness: only through the miss direction d_K, which every scatter
-//     after the first roughness use moves.  Computed here by forward-mode
-//     automatic differentiation: the roughness of the object hit at bounce k
-//     is seeded as tangent slot k of a dual number, and the unchanged path
-//     code (intersection, normal, reflect, refract, normalize, sky) carries
-//     the tangents.  This is a different derivation from the CUDA backward
-//     kernel's hand-written reverse sweep, so the two check each other.
+//   - roughness, two parts:
+//     * pathwise: through the miss direction d_K, which every scatter after
+//       the first roughness use moves.  Computed here by forward-mode
+//       automatic differentiation: the roughness of the object hit at bounce
+//       k is seeded as tangent slot k of a dual number, and the unchanged
+//       path code (intersection, normal, reflect, refract, normalize, sky)
+//       carries the tangents;
+//     * lobe choice (score function): where a coin with a parameter-
+//       dependent probability picked the lobe -- U_rough < roughness^2
+//       (cpu.rs:309) or Schlick's R < U_fresnel (cpu.rs:296-297) -- the
+//       probability P of the outcome taken is evaluated in dual numbers too,
+//       and the path adds (radiance gathered after that vertex's scatter) *
+//       dP/P for every slot.  R depends on the incoming direction, so its
+//       tangents reach the roughness of every earlier bounce.
+//     This is a different derivation from the CUDA backward kernel's
+//     hand-written reverse sweep, so the two check each other.
 // Discrete choices (which object is hit, which lobe, the diffuse flip, the
 // front face) are those of the float path, recorded first and then held
 // fixed: the gradient of the same path-replay estimator the CUDA kernels
@@ -149,10 +158,12 @@ inline V3<Dual> at_value(const V3<Dual>& a, V3<float> v) {
 // double) of those pixels into image (npix*3) when it is not null.  Returns
 // the number of paths whose double evaluation lost a recorded hit (grazing
 // rays; they add no albedo or roughness term).
+// g_rough receives both roughness parts; g_rough_path (when not null) the
+// pathwise part alone.
 inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, uint32_t p0, uint32_t p1,
                                 uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed, uint32_t stream,
                                 const float* dl_dimage, double* g_albedo, double* g_rough, double* g_emission,
-                                double* image) {
+                                double* image, double* g_rough_path = nullptr) {
     uint64_t lost = 0;
     for (uint32_t pix = p0; pix < p1; ++pix) {
         const Ray<float> prim_f = primary_ray(sf, pix % s.width, pix / s.width);
@@ -164,6 +175,8 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
             record_path(sf, prim_f, max_bounces, seed, stream, pix, s0 + k, &rec);
             Ray<Dual> ray = prim;
             bool ok = true;
+            // d log P / d(slot j) of the coin that decided vertex v's lobe (0 without one)
+            double dlogp[kGradSlots][kGradSlots];
             for (int v = 0; v < rec.nv && ok; ++v) {
                 Object<Dual> ob = s.objects[rec.obj[v]];
                 // evaluate at the float path's ray and hit distance, with the
@@ -187,7 +200,9 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
                 uint32_t words[12];
                 bounce_words(seed, stream, pix, s0 + k, (uint32_t)v, words);
                 Ray<Dual> next;
-                scatter(ray, h, ob, words, &next, &rec.ch[v], true);
+                Dual pc;
+                scatter(ray, h, ob, words, &next, &rec.ch[v], true, &pc);
+                for (int j = 0; j < kGradSlots; ++j) dlogp[v][j] = pc.d[j] / pc.v;
                 ray = next;
             }
             double light[3] = {0.0, 0.0, 0.0};
@@ -202,6 +217,35 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
                 }
             }
             if (!ok) ++lost;
+            // radiance gathered after each vertex's scatter: later emission + the sky term
+            double after[kGradSlots][3];
+            if (ok) {
+                double S[3] = {0.0, 0.0, 0.0};
+                if (rec.missed) {
+                    const V3<Dual> sky = world_sample(s, at_value(ray.direction, rec.d_end));
+                    const double sk[3] = {sky.x.v, sky.y.v, sky.z.v};
+                    for (int c = 0; c < 3; ++c) {
+                        double prod = 1.0;
+                        for (int v = 0; v < rec.nv; ++v) {
+                            const V3<Dual>& a = s.objects[rec.obj[v]].albedo;
+                            prod *= c == 0 ? a.x.v : (c == 1 ? a.y.v : a.z.v);
+                        }
+                        S[c] = sk[c] * prod;
+                    }
+                }
+                for (int v = rec.nv - 1; v >= 0; --v) {
+                    for (int c = 0; c < 3; ++c) after[v][c] = S[c];
+                    const Object<Dual>& ob = s.objects[rec.obj[v]];
+                    S[0] += ob.emission_color.x.v * ob.emission_strength.v;
+                    S[1] += ob.emission_color.y.v * ob.emission_strength.v;
+                    S[2] += ob.emission_color.z.v * ob.emission_strength.v;
+                }
+                for (int v = 0; v < rec.nv; ++v) {
+                    const double wv = w[0] * after[v][0] + w[1] * after[v][1] + w[2] * after[v][2];
+                    if (wv == 0.0) continue;
+                    for (int j = 0; j <= v; ++j) g_rough[rec.obj[j]] += wv * dlogp[v][j];
+                }
+            }
             if (rec.missed && ok) {
                 const V3<Dual> sky = world_sample(s, at_value(ray.direction, rec.d_end));
                 const Dual skyc[3] = {sky.x, sky.y, sky.z};
@@ -220,6 +264,7 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
                             if (m != v) others *= alb[m];
                         g_albedo[3 * (size_t)rec.obj[v] + c] += w[c] * skyc[c].v * others;
                         g_rough[rec.obj[v]] += w[c] * prod * skyc[c].d[v];
+                        if (g_rough_path) g_rough_path[rec.obj[v]] += w[c] * prod * skyc[c].d[v];
                     }
                 }
             }

@@ -8,22 +8,39 @@
 // dL/dimage(p) / spp.  Gradients per object:
 //   - emission E = emission_color * emission_strength: the weight, once per hit;
 //   - albedo: weight * sky * the product of the path's other albedos;
-//   - roughness^2 (the host applies d(r^2)/dr = 2r): only through the miss
-//     direction d_K.  The kernel seeds the adjoint of d_K with the sky's
-//     derivative and sweeps the path's vertices in reverse, through the
-//     scatter (normalize, reflect, refract), the front-face flip, the sphere
-//     normal and the ray parameter t (implicit differentiation of the hit
-//     surface), accumulating each vertex's roughness term.
-// Discrete choices (the object hit, the lobe, the diffuse flip) are not
-// differentiated: this is the gradient of the path-replay estimator.
+//   - roughness^2 (the host applies d(r^2)/dr = 2r), two parts:
+//     * pathwise: through the miss direction d_K.  The kernel seeds the
+//       adjoint of d_K with the sky's derivative and sweeps the path's
+//       vertices in reverse, through the scatter (normalize, reflect,
+//       refract), the front-face flip, the sphere normal and the ray
+//       parameter t (implicit differentiation of the hit surface);
+//     * lobe choice (score function): two coins pick a lobe with a
+//       probability that depends on the parameters -- U_rough < r^2 picks
+//       diffuse over specular (cpu.rs:309-313; P = r^2 or 1 - r^2) and
+//       Schlick's R < U_fresnel picks refraction over reflection
+//       (cpu.rs:296-297; P = 1 - R or R, where R depends on the incoming
+//       direction and so on the roughness of every earlier vertex).  A
+//       vertex whose lobe a coin chose adds w_k * d log P / d(params), with
+//       w_k the weighted radiance the path gathers after that choice (the
+//       emission of later hits and the sky term); d log P flows into r^2
+//       directly or, for R, backwards through the incoming ray like the
+//       pathwise part.  In expectation this is the derivative of the lobe
+//       probabilities; it is exact for 0 < roughness < 1.  At roughness 1 (a
+//       lobe that is always diffuse) the specular alternative is never
+//       sampled, so the derivative from below misses its -E[specular] half.
+// Not differentiated: which object a ray hits (a roughness step can move a
+// ray across another object's silhouette: a boundary term), the diffuse
+// flip and the total-internal-reflection edge.
 //
 // Nothing of the forward pass is stored: each path is replayed from its
 // Philox counter (pixel, sample, bounce) with the forward kernels' own
 // functions, so it retraces the rendered path bit for bit, into a per-thread
-// record of at most kAdjMaxBounces vertices.  Gradients are summed per warp
-// over lanes that hit the same object (match + pointer-jumping reduction)
-// and added with FP32 atomics, into per-block shared accumulators when the
-// scene's gradient table fits, else straight into global memory.
+// record of at most kAdjMaxBounces vertices of 32 bytes (incoming ray, hit
+// distance, object and scatter flags); the reverse sweep recomputes the
+// lobe's unit-sphere vector from the same counter.  Gradients are summed per
+// warp over lanes that hit the same object (match + pointer-jumping
+// reduction) and added with FP32 atomics, into per-block shared accumulators
+// when the scene's gradient table fits, else straight into global memory.
 #include <cstdint>
 
 #include "rdc_bvh.cuh"
@@ -33,24 +50,34 @@ namespace rdc {
 
 namespace {
 
+// One vertex of a replayed path (32 bytes): the ray that reaches it, its
+// hit distance and the object index (low 24 bits) with the scatter flags
+// (high 8).  After the reverse sweep o holds the vertex's albedo gradient
+// without the albedos before it, and t its dL/d(roughness^2).
 struct AdjVert {
-    V3 o, d;       // incoming ray
-    float t;       // hit distance; after the sweep: dL/d(roughness^2) of this vertex
-    int obj;
-    uint32_t flags;  // ScatterRec flags
-    V3 s;          // unit-sphere vector of the lobe
-    V3 pre;        // product of the albedos before this vertex; after the sweep: dL/dalbedo
+    V3 o, d;
+    float t;
+    uint32_t objf;
 };
 
+__device__ __forceinline__ V3 vjp_normalize(V3 v, V3 u, float len, V3 g) {
+    // u = v / len: du = (dv - u (u . dv)) / len
+    (void)v;
+    return vmul(vsub(g, vmul(u, vdot(g, u))), 1.0f / len);
+}
+
 // Reverse step through vertex v: (go, gd) are the adjoints of the ray that
-// leaves v; returns those of the ray that reaches v and dL/d(roughness^2).
-__device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& v, V3& go, V3& gd) {
-    const MatDev m = load_mat(sc.mat, v.obj);
-    const float4 hi = __ldg(&sc.hit[v.obj]);
+// leaves v; on return those of the ray that reaches v.  s is the lobe's
+// unit-sphere vector, wk the weighted radiance gathered after the vertex's
+// scatter (for the coin terms).  Returns dL/d(roughness^2) of this vertex.
+__device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& v, const MatDev& m, V3 s,
+                                            float wk, V3& go, V3& gd) {
+    const int obj = (int)(v.objf & 0xFFFFFFu);
+    const uint32_t f = v.objf >> 24;
+    const float4 hi = __ldg(&sc.hit[obj]);
     const int kind = __float_as_int(m.d.y);
     const HitRec h = closest_hit(v.o, v.d, v.t, hi, kind);
     const float r = m.a.w;
-    const uint32_t f = v.flags;
     const V3 d = v.d, n = h.n;
     V3 g_dir = mk(0.f, 0.f, 0.f), g_n = mk(0.f, 0.f, 0.f);
     if (f & kScatNormal)
@@ -64,47 +91,69 @@ __device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& 
     V3 g_p = go, g_din = mk(0.f, 0.f, 0.f);
     float gr = 0.0f;
     const uint32_t lobe = f & 3u;
+
+    // U_rough < r^2: P(diffuse) = r^2, P(specular) = 1 - r^2
+    if (f & kScatRoughCoin) gr += lobe == kLobeDiffuse ? wk / r : -wk / (1.0f - r);
+
+    // Fresnel quantities of a transmission vertex: rd = d / |d|,
+    // cos = min(-rd.n, 1), R = r0 + (1 - r0)(1 - cos)^5
+    float dl = 1.0f, cr = 0.0f, cs = 0.0f, g_cs = 0.0f;
+    V3 rd = d;
+    if (f & kScatTrans) {
+        dl = sqrtf(vdot(d, d));
+        rd = vmul(d, 1.0f / dl);
+        cr = -vdot(rd, n);
+        cs = fminf(cr, 1.0f);
+        if (f & kScatFresnelCoin) {
+            const float r0 = (f & kScatFront) ? m.c.w : m.d.x;
+            const float mm = 1.0f - cs;
+            const float m2 = mm * mm;
+            const float R = r0 + (1.0f - r0) * (mm * (m2 * m2));
+            const float gR = lobe == kLobeRefract ? -wk / (1.0f - R) : wk / R;
+            g_cs = gR * (-5.0f * (1.0f - r0) * (m2 * m2));
+        }
+    }
+
     if (lobe == kLobeDiffuse) {
         g_n = (f & kScatFlip) ? vsub(g_n, g_dir) : vadd(g_n, g_dir);  // dir = +-(n + s1)
     } else if (lobe == kLobeSpecular) {
         // dir = X / |X|, X = d - 2 (d.n) n + s2 r
         const float dn = vdot(d, n);
-        const V3 X = vadd(vsub(d, vmul(n, 2.0f * dn)), vmul(v.s, r));
+        const V3 X = vadd(vsub(d, vmul(n, 2.0f * dn)), vmul(s, r));
         const float L = sqrtf(vdot(X, X));
-        const V3 u = vmul(X, 1.0f / L);
-        const V3 gX = vmul(vsub(g_dir, vmul(u, vdot(g_dir, u))), 1.0f / L);
-        gr += vdot(v.s, gX);
+        const V3 gX = vjp_normalize(X, vmul(X, 1.0f / L), L, g_dir);
+        gr += vdot(s, gX);
         const float ngX = vdot(n, gX);
         g_din = vadd(g_din, vsub(gX, vmul(n, 2.0f * ngX)));
         g_n = vsub(g_n, vadd(vmul(gX, 2.0f * dn), vmul(d, 2.0f * ngX)));
+        if ((f & kScatTrans) && cr < 1.0f && g_cs != 0.0f) {
+            // a reflection the Fresnel coin chose: R's cos through rd and n
+            g_n = vsub(g_n, vmul(rd, g_cs));
+            g_din = vadd(g_din, vjp_normalize(d, rd, dl, vmul(n, -g_cs)));
+        }
     } else {
         // dir = Z / |Z|, Z = perp + s n + s3 r, perp = ratio (rd + cos n),
         // s = -sqrt|1 - perp.perp|, cos = min(-rd.n, 1), rd = d / |d|
         const float ratio = (f & kScatFront) ? m.c.y : m.c.z;
-        const float dl = sqrtf(vdot(d, d));
-        const V3 rd = vmul(d, 1.0f / dl);
-        const float cr = -vdot(rd, n);
-        const float cs = fminf(cr, 1.0f);
         const V3 perp = vmul(vadd(rd, vmul(n, cs)), ratio);
         const float q = 1.0f - vdot(perp, perp);
         const float sq = sqrtf(fabsf(q));
-        const V3 Z = vadd(vadd(perp, vmul(n, -sq)), vmul(v.s, r));
+        const V3 Z = vadd(vadd(perp, vmul(n, -sq)), vmul(s, r));
         const float L = sqrtf(vdot(Z, Z));
-        const V3 u = vmul(Z, 1.0f / L);
-        const V3 gZ = vmul(vsub(g_dir, vmul(u, vdot(g_dir, u))), 1.0f / L);
-        gr += vdot(v.s, gZ);
+        const V3 gZ = vjp_normalize(Z, vmul(Z, 1.0f / L), L, g_dir);
+        gr += vdot(s, gZ);
         V3 g_perp = gZ;
         const float gs = vdot(n, gZ);
         g_n = vadd(g_n, vmul(gZ, -sq));
         if (sq > 1e-12f) g_perp = vadd(g_perp, vmul(perp, gs * (q < 0.0f ? -1.0f : 1.0f) / sq));
         V3 g_rd = vmul(g_perp, ratio);
-        const float gcos = ratio * vdot(n, g_perp);
+        const float gcos = ratio * vdot(n, g_perp) + g_cs;
         g_n = vadd(g_n, vmul(g_perp, ratio * cs));
         if (cr < 1.0f) {
             g_rd = vsub(g_rd, vmul(n, gcos));
             g_n = vsub(g_n, vmul(rd, gcos));
         }
-        g_din = vadd(g_din, vmul(vsub(g_rd, vmul(rd, vdot(g_rd, rd))), 1.0f / dl));
+        g_din = vadd(g_din, vjp_normalize(d, rd, dl, g_rd));
     }
     // n = +-n0 (front-face flip); sphere n0 = (p - c) / |p - c|, cube n0 constant
     const V3 g_n0 = h.front ? g_n : vneg(g_n);
@@ -113,7 +162,7 @@ __device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& 
     if (kind == 0) {
         const float pl = sqrtf(vdot(pc, pc));
         const V3 n0 = vmul(pc, 1.0f / pl);
-        g_p = vadd(g_p, vmul(vsub(g_n0, vmul(n0, vdot(g_n0, n0))), 1.0f / pl));
+        g_p = vadd(g_p, vjp_normalize(pc, n0, pl, g_n0));
     }
     // p = o + t d with t(o, d) on the hit surface
     const float g_t = vdot(g_p, d);
@@ -253,18 +302,18 @@ __global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParam
                     vk.o = o;
                     vk.d = d;
                     vk.t = t;
-                    vk.obj = idx;
-                    vk.flags = rec.flags;
-                    vk.s = rec.s;
-                    vk.pre = atten;
+                    vk.objf = (uint32_t)idx | (rec.flags << 24);
                     atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
                     o = no;
                     d = nd;
                 }
-                // reverse sweep
+                // reverse sweep: S = the radiance gathered after the current
+                // vertex's scatter, suf = the albedos after it
+                V3 go = mk(0.f, 0.f, 0.f), gd = mk(0.f, 0.f, 0.f);
+                V3 sky = mk(0.f, 0.f, 0.f), S = mk(0.f, 0.f, 0.f);
                 if (missed) {
-                    const V3 sky = world_sample(P.sc, d);
-                    V3 go = mk(0.f, 0.f, 0.f), gd = mk(0.f, 0.f, 0.f);
+                    sky = world_sample(P.sc, d);
+                    S = mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z);
                     if (P.sc.world_kind == 0u) {
                         // sky = bottom + (top - bottom) (d.y / |d| + 1) / 2
                         const float coef = 0.5f * (gw.x * atten.x * (P.sc.top[0] - P.sc.bottom[0]) +
@@ -274,37 +323,53 @@ __global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParam
                         const float cosv = d.y / len;
                         gd = vmul(vsub(mk(0.f, 1.f, 0.f), vmul(d, cosv / len)), coef / len);
                     }
-                    V3 suf = mk(1.f, 1.f, 1.f);
-                    for (int k = nv - 1; k >= 0; --k) {
-                        AdjVert& vk = v[k];
-                        const float4 alb = P.sc.mat[vk.obj].a;
-                        const V3 ga = mk(gw.x * sky.x * vk.pre.x * suf.x, gw.y * sky.y * vk.pre.y * suf.y,
-                                         gw.z * sky.z * vk.pre.z * suf.z);
-                        suf = mk(suf.x * alb.x, suf.y * alb.y, suf.z * alb.z);
-                        vk.t = vertex_vjp(P.sc, vk, go, gd);
-                        vk.pre = ga;
+                }
+                const uint32_t pix_s = pix;
+                V3 suf = mk(1.f, 1.f, 1.f);
+                for (int k = nv - 1; k >= 0; --k) {
+                    AdjVert& vk = v[k];
+                    const int obj = (int)(vk.objf & 0xFFFFFFu);
+                    const uint32_t f = vk.objf >> 24;
+                    const MatDev m = load_mat(P.sc.mat, obj);
+                    // the lobe's unit-sphere vector: s2 from words 3-5, s3 from words 8-10
+                    V3 s = mk(0.f, 0.f, 0.f);
+                    const uint32_t lobe = f & 3u;
+                    if (lobe == kLobeSpecular) {
+                        const U4 a = philox(pix_s, sample, (uint32_t)k * 4u, P.stream_id, P.key0, P.key1);
+                        const U4 b = philox(pix_s, sample, (uint32_t)k * 4u + 1u, P.stream_id, P.key0, P.key1);
+                        s = unit_sphere(a.w, b.x, b.y);
+                    } else if (lobe == kLobeRefract) {
+                        const U4 c = philox(pix_s, sample, (uint32_t)k * 4u + 2u, P.stream_id, P.key0, P.key1);
+                        s = unit_sphere(c.x, c.y, c.z);
                     }
-                } else {
-                    for (int k = 0; k < nv; ++k) {
-                        v[k].t = 0.0f;
-                        v[k].pre = mk(0.f, 0.f, 0.f);
-                    }
+                    const float wk = gw.x * S.x + gw.y * S.y + gw.z * S.z;
+                    const float gr = vertex_vjp(P.sc, vk, m, s, wk, go, gd);
+                    vk.o = mk(gw.x * sky.x * suf.x, gw.y * sky.y * suf.y, gw.z * sky.z * suf.z);
+                    vk.t = gr;
+                    suf = mk(suf.x * m.a.x, suf.y * m.a.y, suf.z * m.a.z);
+                    S = mk(S.x + m.b.x, S.y + m.b.y, S.z + m.b.z);
                 }
             }
         }
-        // warp-converged accumulation over vertex slots
+        // warp-converged accumulation over vertex slots; pre = the albedos
+        // before vertex k, which completes its albedo gradient
         const int maxnv = (int)__reduce_max_sync(FULL, (unsigned)nv);
+        V3 pre = mk(1.f, 1.f, 1.f);
         for (int k = 0; k < maxnv; ++k) {
             const bool has = k < nv;
-            const int obj = has ? v[k].obj : -1;
+            const int obj = has ? (int)(v[k].objf & 0xFFFFFFu) : -1;
             float c[7];
-            c[0] = has ? v[k].pre.x : 0.0f;
-            c[1] = has ? v[k].pre.y : 0.0f;
-            c[2] = has ? v[k].pre.z : 0.0f;
+            c[0] = has ? v[k].o.x * pre.x : 0.0f;
+            c[1] = has ? v[k].o.y * pre.y : 0.0f;
+            c[2] = has ? v[k].o.z * pre.z : 0.0f;
             c[3] = has ? gw.x : 0.0f;
             c[4] = has ? gw.y : 0.0f;
             c[5] = has ? gw.z : 0.0f;
             c[6] = has ? v[k].t : 0.0f;
+            if (has) {
+                const float4 alb = __ldg(&P.sc.mat[obj].a);
+                pre = mk(pre.x * alb.x, pre.y * alb.y, pre.z * alb.z);
+            }
             warp_add_grad(gbase, obj, c);
         }
     }

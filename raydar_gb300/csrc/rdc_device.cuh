@@ -554,8 +554,10 @@ __device__ __forceinline__ V3 unit_sphere(uint32_t a, uint32_t b, uint32_t c) {
 }
 
 // What the adjoint needs to replay a scatter backwards: the lobe taken, the
-// diffuse flip, the transmission offset, the |dir| < 1e-5 fallback, and the
-// unit-sphere vector the lobe added (scaled by roughness^2).
+// diffuse flip, the transmission offset, the |dir| < 1e-5 fallback, which
+// coin with a parameter-dependent probability decided the lobe, and the
+// unit-sphere vector the lobe added (scaled by roughness^2).  The flags fit
+// in 8 bits.
 enum : uint32_t {
     kLobeDiffuse = 0u,
     kLobeSpecular = 1u,
@@ -564,6 +566,8 @@ enum : uint32_t {
     kScatTrans = 8u,     // transmission ray: origin offset along the new direction
     kScatNormal = 16u,   // |dir|^2 < 1e-10: the new direction is the normal
     kScatFront = 32u,    // the hit's front-face flag
+    kScatRoughCoin = 64u,    // U_rough < roughness^2 chose diffuse or specular (cpu.rs:309-313)
+    kScatFresnelCoin = 128u, // Schlick's R < U_fresnel chose refraction or reflection (cpu.rs:296-297)
 };
 struct ScatterRec {
     uint32_t flags;
@@ -590,6 +594,7 @@ __device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev
     const V3 s2 = unit_sphere(w[3], w[4], w[5]);
     const V3 specular = vnormalize(vadd(perfect, vmul(s2, rough)));
     uint32_t lobe = kLobeSpecular;
+    uint32_t coin = 0u;
     V3 s_used = s2;
 
     const bool trans = u01(w[6]) < transmission;
@@ -605,10 +610,14 @@ __device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev
         const float m5 = mm * (m2 * m2);
         const float refl = r0 + (1.0f - r0) * m5;
         bool refracted = false;
-        if (refl < u01(w[7])) {
+        const bool coin_refracts = refl < u01(w[7]);
+        if (coin_refracts || Rec) {  // the recording form also needs it when the coin says reflect
             // can_refract, src/utils/mod.rs:37-44
             const float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
-            refracted = ratio * sin_theta <= 1.0f;
+            const bool can = ratio * sin_theta <= 1.0f;
+            refracted = coin_refracts && can;
+            // under total internal reflection the lobe is reflection whatever the coin says
+            coin = can ? kScatFresnelCoin : 0u;
         }
         if (refracted) {
             // refract, src/utils/mod.rs:25-35
@@ -627,8 +636,10 @@ __device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev
     } else if (u01(w[8]) < rough) {
         dir = diffuse;
         lobe = kLobeDiffuse;
+        coin = kScatRoughCoin;
     } else {
         dir = specular;
+        coin = kScatRoughCoin;
     }
     const V3 off = trans ? dir : h.n;
     o_out = vadd(h.p, vmul(off, 0.0001f));
@@ -636,7 +647,7 @@ __device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev
     d_out = to_normal ? h.n : dir;
     if (Rec) {
         rec->flags = lobe | (flip ? kScatFlip : 0u) | (trans ? kScatTrans : 0u) | (to_normal ? kScatNormal : 0u) |
-                     (h.front ? kScatFront : 0u);
+                     (h.front ? kScatFront : 0u) | coin;
         rec->s = s_used;
     }
 }

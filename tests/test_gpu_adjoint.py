@@ -4,9 +4,11 @@ finite differences of the CUDA forward image with common random numbers.
 
 Tolerances: relative L2 error of each gradient table below 1e-2 against the
 FP64 oracle; albedo and emission within 1e-3 of central differences (the
-image is polynomial in them); roughness differences include visibility and
-lobe changes that path replay leaves out, so that gap is bounded loosely and
-printed."""
+image is polynomial in them).  On this cluttered scene a roughness step also
+moves rays across other objects' silhouettes, a boundary term the estimator
+leaves out, so the roughness difference quotient here is only printed; the
+roughness gradient is checked against central differences where they are
+well defined in test_gpu_roughness_gradient.py."""
 import numpy as np
 import pytest
 import torch
@@ -96,11 +98,10 @@ def test_albedo_and_emission_match_central_differences(grads):
 
 
 def test_roughness_central_difference_gap_is_stated(grads):
-    """A roughness step moves scatter directions and also flips some paths'
-    hit object or lobe; those jumps are in the difference quotient but not in
-    the path-replay gradient (whose interior part the FP64 oracle pins, and
-    which the oracle's own double-precision differences confirm).  The gap is
-    printed, not bounded."""
+    """A roughness step moves scatter directions across other objects'
+    silhouettes; those jumps are in the difference quotient but not in the
+    estimator (which the FP64 oracle pins).  At 16 spp the quotient is also
+    dominated by coin flips.  The gap is printed, not bounded."""
     scene, img, dl, (ga, gr, ge), _, _ = grads
     alb, rough, em = (t.numpy() for t in material_tensors(scene))
     metals = [i for i, o in enumerate(scene.objects) if o.material.metallic == 1.0 and o.material.roughness > 0.1]

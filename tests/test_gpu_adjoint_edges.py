@@ -68,7 +68,11 @@ def test_adjoint_on_an_lbvh_scene_matches_the_fp64_oracle():
             assert np.linalg.norm(g - o) / np.linalg.norm(o) < 1e-2
 
 
-def test_solid_color_world_has_no_roughness_gradient():
+def test_solid_color_world_has_only_the_lobe_choice_roughness_gradient():
+    """Under a SolidColor world no direction changes a path's radiance, so the
+    pathwise part of the roughness gradient is zero; what remains is the
+    lobe-choice part (which lobe a coin picks changes what the path hits
+    next), and the kernel's must equal the FP64 oracle's."""
     scene = shrink(scenegen.c4_diff().scene, 24, 24)
     scene.world = World("SolidColor", color=np.array([0.6, 0.7, 0.8], np.float32))
     r = CudaRenderer(RendererConfig(max_bounces=6), seed=2)
@@ -76,9 +80,11 @@ def test_solid_color_world_has_no_roughness_gradient():
     dl = np.ones((24, 24, 3), np.float32)
     ga, gr, ge = r.backward(scene, dl)
     r.close()
-    assert np.all(gr == 0) and np.abs(ga).sum() > 0 and np.abs(ge).sum() > 0
-    oa, orr, oe, _ = oracle.gradient(scene.to_c(), 0, 4, 6, 2, dl, threads=8)
+    assert np.abs(ga).sum() > 0 and np.abs(ge).sum() > 0
+    oa, orr, oe, _, path = oracle.gradient(scene.to_c(), 0, 4, 6, 2, dl, threads=8, pathwise=True)
+    assert np.all(path == 0.0) and np.abs(orr).sum() > 0
     assert np.linalg.norm(ga - oa) / np.linalg.norm(oa) < 1e-4
+    assert np.linalg.norm(gr - orr) / np.linalg.norm(orr) < 1e-3
 
 
 def test_adjoint_bounce_limit_and_material_count_are_checked():

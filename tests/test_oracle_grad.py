@@ -4,7 +4,12 @@ double-precision image (same Philox words, i.e. common random numbers).
 Albedo and emission enter a path's radiance polynomially, so central
 differences match the analytic gradient to rounding.  Roughness moves scatter
 directions; with a small step no path changes its hit sequence or lobe, and
-the forward-mode tangents must match the difference quotient closely."""
+the pathwise part of the roughness gradient (the forward-mode tangents of the
+miss direction) must match the difference quotient closely.  The lobe-choice
+part is a score-function term whose mean is the derivative of the lobe
+probabilities: a small step with common random numbers flips no coin, so it
+is checked against the CUDA adjoint and, at many samples, against central
+differences of the GPU render instead."""
 import copy
 
 import numpy as np
@@ -25,8 +30,8 @@ def setup():
     scene = shrink(scenegen.c4_diff().scene, W, H)
     rng = np.random.default_rng(5)
     dl = rng.uniform(-1.0, 1.0, (H, W, 3)).astype(np.float32)
-    ga, gr, ge, img = oracle.gradient(scene.to_c(), 0, SPP, BOUNCES, SEED, dl, threads=8)
-    return scene, dl, ga, gr, ge, img
+    ga, gr, ge, img, gp = oracle.gradient(scene.to_c(), 0, SPP, BOUNCES, SEED, dl, threads=8, pathwise=True)
+    return scene, dl, ga, gr, ge, img, gp
 
 
 def _loss(scene, dl):
@@ -44,7 +49,7 @@ def _fd(scene, dl, set_param, base, eps):
 
 
 def test_image_matches_the_float_oracle(setup):
-    scene, dl, ga, gr, ge, img = setup
+    scene, dl, ga, gr, ge, img, gp = setup
     acc, _ = oracle.render(scene.to_c(), 0, SPP, BOUNCES, SEED, threads=8)
     ref = acc[..., :3].astype(np.float64) / SPP
     # the double path follows the float path except on rare borderline decisions
@@ -53,7 +58,7 @@ def test_image_matches_the_float_oracle(setup):
 
 
 def test_albedo_and_emission_gradients_match_central_differences(setup):
-    scene, dl, ga, gr, ge, img = setup
+    scene, dl, ga, gr, ge, img, gp = setup
     checked = 0
     for j in (0, 3, 11):  # the ground and two spheres
         for c in range(3):
@@ -78,15 +83,29 @@ def test_albedo_and_emission_gradients_match_central_differences(setup):
 
 
 def test_metal_roughness_gradient_matches_central_differences(setup):
-    scene, dl, ga, gr, ge, img = setup
+    scene, dl, ga, gr, ge, img, gp = setup
     metals = [i for i, o in enumerate(scene.objects)
-              if o.material.metallic == 1.0 and o.material.roughness > 0.1 and abs(gr[i]) > 0]
+              if o.material.metallic == 1.0 and o.material.roughness > 0.1 and abs(gp[i]) > 0]
     assert metals, "the scene has a rough metal that the image sees"
-    j = max(metals, key=lambda i: abs(gr[i]))
+    j = max(metals, key=lambda i: abs(gp[i]))
     base = float(scene.objects[j].material.roughness)
 
     def set_r(s, v):
         s.objects[j].material.roughness = float(v)
 
     fd = _fd(scene, dl, set_r, base, 1e-5)
-    assert abs(fd - gr[j]) <= 2e-2 * abs(gr[j]), (j, fd, gr[j])
+    assert abs(fd - gp[j]) <= 2e-2 * abs(gp[j]), (j, fd, gp[j])
+
+
+def test_lobe_choice_terms_are_separate_from_the_pathwise_part(setup):
+    """Objects of the Specular class (roughness 0.5, not metal, not glass)
+    take the roughness coin on every hit, so their gradient has a lobe term;
+    metals take no roughness coin, so theirs differs from the pathwise part
+    only through the Fresnel coins of glass hits further along the path."""
+    scene, dl, ga, gr, ge, img, gp = setup
+    spec = [i for i, o in enumerate(scene.objects) if o.material.metallic == 0.0 and
+            o.material.transmission == 0.0 and o.material.roughness == 0.5]
+    assert spec and any(abs(gr[i] - gp[i]) > 1e-9 * (1 + abs(gr[i])) for i in spec)
+    # objects with roughness 0 (glass) have no roughness gradient of either kind: d(r^2)/dr = 0 there
+    glass = [i for i, o in enumerate(scene.objects) if o.material.roughness == 0.0]
+    assert glass and all(gr[i] == 0.0 and gp[i] == 0.0 for i in glass)
