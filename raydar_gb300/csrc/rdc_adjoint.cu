@@ -35,9 +35,10 @@
 // Nothing of the forward pass is stored: each path is replayed from its
 // Philox counter (pixel, sample, bounce) with the forward kernels' own
 // functions, so it retraces the rendered path bit for bit, into a per-thread
-// record of at most kAdjMaxBounces vertices of 32 bytes (incoming ray, hit
-// distance, object and scatter flags); the reverse sweep recomputes the
-// lobe's unit-sphere vector from the same counter.  Gradients are summed per
+// record of at most kAdjMaxBounces vertices of 44 bytes (incoming ray, hit
+// distance, object and scatter flags, the lobe's unit-sphere vector; keeping
+// the vector measured 13% faster than recomputing its Philox words in the
+// sweep).  Gradients are summed per
 // warp over lanes that hit the same object (match + pointer-jumping
 // reduction) and added with FP32 atomics, into per-block shared accumulators
 // when the scene's gradient table fits, else straight into global memory.
@@ -50,14 +51,16 @@ namespace rdc {
 
 namespace {
 
-// One vertex of a replayed path (32 bytes): the ray that reaches it, its
-// hit distance and the object index (low 24 bits) with the scatter flags
-// (high 8).  After the reverse sweep o holds the vertex's albedo gradient
-// without the albedos before it, and t its dL/d(roughness^2).
+// One vertex of a replayed path (44 bytes): the ray that reaches it, its
+// hit distance, the object index (low 24 bits) with the scatter flags (high
+// 8) and the unit-sphere vector the lobe added.  After the reverse sweep o
+// holds the vertex's albedo gradient without the albedos before it, and t
+// its dL/d(roughness^2).
 struct AdjVert {
     V3 o, d;
     float t;
     uint32_t objf;
+    V3 s;
 };
 
 __device__ __forceinline__ V3 vjp_normalize(V3 v, V3 u, float len, V3 g) {
@@ -232,8 +235,14 @@ __device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7]) {
     }
 }
 
+// Resident blocks per SM the register budget is sized for (64 registers at 4;
+// 3, 4 and 5 measured within 2% of each other on config 4, 4 the fastest).
+#ifndef RDC_ADJ_MIN_BLOCKS
+#define RDC_ADJ_MIN_BLOCKS 4
+#endif
+
 template <bool kBvh>
-__global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParams P) {
+__global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kernel(const AdjParams P) {
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
     float4* s_rec = smem;
@@ -272,6 +281,7 @@ __global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParam
                 primary_ray(P.sc, pix % P.sc.width, pix / P.sc.width, o, d);
                 V3 atten = mk(1.f, 1.f, 1.f);
                 bool missed = false;
+                bool emit_after_first = false;  // an emissive hit after vertex 0
                 for (uint32_t b = 0; b < P.max_bounces; ++b) {
                     ++segs;
                     const RayPre r = ray_pre(o, d, P.sc.neg_zero);
@@ -303,10 +313,16 @@ __global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParam
                     vk.d = d;
                     vk.t = t;
                     vk.objf = (uint32_t)idx | (rec.flags << 24);
+                    vk.s = rec.s;
                     atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
+                    emit_after_first = emit_after_first || (b > 0u && (m.b.x != 0.0f || m.b.y != 0.0f || m.b.z != 0.0f));
                     o = no;
                     d = nd;
                 }
+                // A path that ends without a miss gathers only emission: with no
+                // emissive hit after its first vertex every coin weight is zero
+                // and nothing depends on a direction, so its sweep adds nothing.
+                const bool sweep = missed || emit_after_first;
                 // reverse sweep: S = the radiance gathered after the current
                 // vertex's scatter, suf = the albedos after it
                 V3 go = mk(0.f, 0.f, 0.f), gd = mk(0.f, 0.f, 0.f);
@@ -324,24 +340,18 @@ __global__ void __launch_bounds__(kRenderBlock, 5) adjoint_kernel(const AdjParam
                         gd = vmul(vsub(mk(0.f, 1.f, 0.f), vmul(d, cosv / len)), coef / len);
                     }
                 }
-                const uint32_t pix_s = pix;
                 V3 suf = mk(1.f, 1.f, 1.f);
-                for (int k = nv - 1; k >= 0; --k) {
+                if (!sweep) {
+                    for (int k = 0; k < nv; ++k) {
+                        v[k].o = mk(0.f, 0.f, 0.f);
+                        v[k].t = 0.0f;
+                    }
+                }
+                for (int k = sweep ? nv - 1 : -1; k >= 0; --k) {
                     AdjVert& vk = v[k];
                     const int obj = (int)(vk.objf & 0xFFFFFFu);
-                    const uint32_t f = vk.objf >> 24;
                     const MatDev m = load_mat(P.sc.mat, obj);
-                    // the lobe's unit-sphere vector: s2 from words 3-5, s3 from words 8-10
-                    V3 s = mk(0.f, 0.f, 0.f);
-                    const uint32_t lobe = f & 3u;
-                    if (lobe == kLobeSpecular) {
-                        const U4 a = philox(pix_s, sample, (uint32_t)k * 4u, P.stream_id, P.key0, P.key1);
-                        const U4 b = philox(pix_s, sample, (uint32_t)k * 4u + 1u, P.stream_id, P.key0, P.key1);
-                        s = unit_sphere(a.w, b.x, b.y);
-                    } else if (lobe == kLobeRefract) {
-                        const U4 c = philox(pix_s, sample, (uint32_t)k * 4u + 2u, P.stream_id, P.key0, P.key1);
-                        s = unit_sphere(c.x, c.y, c.z);
-                    }
+                    const V3 s = vk.s;
                     const float wk = gw.x * S.x + gw.y * S.y + gw.z * S.z;
                     const float gr = vertex_vjp(P.sc, vk, m, s, wk, go, gd);
                     vk.o = mk(gw.x * sky.x * suf.x, gw.y * sky.y * suf.y, gw.z * sky.z * suf.z);
