@@ -11,7 +11,7 @@ scenes/benchmark.rscn) and writes, next to this script:
                            reference's own 3840x2160, 183-object benchmark scene)
 Values are kept exactly as parsed (Python floats of the file's decimal text).
 
-Run in a checkout that has the reference: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT   (the root of a raydar checkout)
 """
 import json
 import sys
@@ -20,8 +20,10 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str) -> None:
     ref = Path(ref_root)
+    if not (ref / "scenes" / "default.rscn").exists():
+        raise SystemExit(f"{ref}: not a raydar checkout (no scenes/default.rscn)")
     cams = {}
     for name in ("default", "benchmark"):
         data = json.loads((ref / "scenes" / f"{name}.rscn").read_text())
@@ -31,4 +33,6 @@ def main(ref_root: str = "/root/reference") -> None:
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        raise SystemExit(__doc__)
+    main(sys.argv[1])
