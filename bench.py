@@ -68,6 +68,7 @@ def _args():
     p.add_argument("--wavefront-only", action="store_true", help="only the megakernel / wavefront A/B")
     p.add_argument("--inverse", action="store_true",
                    help="only the config 5 inverse-rendering run (200 Adam steps on 1000 albedos)")
+    p.add_argument("--no-inverse", action="store_true", help="skip the config 5 inverse-rendering run")
     p.add_argument("--batch-spp-div", type=int, default=1, help="divide every batch item's spp (small profiling case)")
     return p.parse_args()
 
@@ -807,6 +808,10 @@ def run_ours(args):
     if rank == 0 and not args.no_progressive:
         progressive = progressive_bench(local)
 
+    inverse = None
+    if rank == 0 and not args.no_inverse:
+        inverse = inverse_bench(local)
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(w, args.cpu_seconds)
@@ -841,6 +846,9 @@ def run_ours(args):
             "bound": "fp32", "kernel": "render_kernel", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak if peak > 0 else None,
             "traffic": traffic,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one 1080p render_kernel launch from "
+                              "the committed ncu capture (profiles/render_kernel_traffic.json), not measured in this "
+                              "run; per pixel, independent of spp",
             "ops_per_segment": ops,
             "peak_source": f"max of the FFMA issue rate measured in this run ({peak_probe:.2f} T lane-ops/s, "
                            f"= {mhz.value:.0f} MHz x {n_sms} SMs x 128) and {n_sms} SMs x 128 x the median "
@@ -858,6 +866,7 @@ def run_ours(args):
         "wavefront_ab": wavefront,
         "reference_benchmark_scene": refscene,
         "progressive": progressive,
+        "inverse": inverse,
     }
     print(json.dumps(line), flush=True)
 

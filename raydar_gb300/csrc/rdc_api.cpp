@@ -8,7 +8,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -130,7 +132,7 @@ rdc_status ensure(rdc_ctx* ctx, T** ptr, size_t* cap, size_t n, const char* what
     if (*ptr) cudaFree(*ptr);
     *ptr = nullptr;
     *cap = 0;
-    cudaError_t e = cudaMalloc((void**)ptr, n * sizeof(T));
+    cudaError_t e = rdc::dev_malloc((void**)ptr, n * sizeof(T));
     if (e != cudaSuccess) return cuda_fail(ctx, e, what);
     *cap = n;
     return RDC_OK;
@@ -248,6 +250,33 @@ rdc_status apply_accel(rdc_ctx* ctx, bool scene_changed) {
 
 namespace rdc {
 void set_thread_error(const std::string& msg) { g_create_error = msg; }
+
+namespace {
+std::mutex g_alloc_mutex;
+bool g_alloc_inject = false;      // RDC_FAIL_ALLOC_AFTER was set at the last rdc_create
+unsigned long long g_alloc_left = 0;  // allocations that still succeed
+}  // namespace
+
+void reset_alloc_injection() {
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    const char* v = std::getenv("RDC_FAIL_ALLOC_AFTER");
+    g_alloc_inject = v != nullptr && *v != '\0';
+    g_alloc_left = g_alloc_inject ? std::strtoull(v, nullptr, 10) : 0;
+}
+
+cudaError_t dev_malloc(void** ptr, size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lock(g_alloc_mutex);
+        if (g_alloc_inject) {
+            if (g_alloc_left == 0) {
+                *ptr = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            --g_alloc_left;
+        }
+    }
+    return cudaMalloc(ptr, bytes);
+}
 }  // namespace rdc
 
 extern "C" {
@@ -279,6 +308,7 @@ rdc_status rdc_create(rdc_ctx** out, int device) {
                          " is not a Blackwell (sm_10x) GPU; this library is built for sm_103a only";
         return RDC_ERR_UNSUPPORTED;
     }
+    rdc::reset_alloc_injection();
     rdc_ctx* ctx = new rdc_ctx();
     ctx->device = device;
     ctx->num_sms = prop.multiProcessorCount;
@@ -292,7 +322,7 @@ rdc_status rdc_create(rdc_ctx** out, int device) {
         return bail(e, "cudaStreamCreate");
     if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
-    if ((e = cudaMalloc((void**)&ctx->d_counters, kCounters * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = rdc::dev_malloc((void**)&ctx->d_counters, kCounters * sizeof(unsigned long long))) != cudaSuccess)
         return bail(e, "cudaMalloc(counters)");
     if ((e = cudaMemset(ctx->d_counters, 0, kCounters * sizeof(unsigned long long))) != cudaSuccess)
         return bail(e, "cudaMemset(counters)");
@@ -357,6 +387,10 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     const bool fast_div = rdc::flatten(sc, rec.data(), hit.data(), mat.data(), runs.data());
 
     if (rdc_status st = set_device(ctx)) return st;
+    // From here on the old scene's buffers may be freed or replaced: a failure
+    // below must leave the context with no scene, never with stale pointers.
+    ctx->has_scene = false;
+    ctx->adj_valid = false;
     if (rdc_status st = ensure(ctx, &ctx->d_rec, &ctx->cap_rec, rec.size(), "cudaMalloc(records)")) return st;
     size_t cap = ctx->cap_obj;
     if (rdc_status st = ensure(ctx, &ctx->d_hit, &cap, hit.size(), "cudaMalloc(hit)")) return st;
@@ -391,7 +425,7 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
         if (ctx->d_accum) cudaFree(ctx->d_accum);
         ctx->d_accum = nullptr;
         const size_t npix = (size_t)cam.resolution_x * cam.resolution_y;
-        cudaError_t e = cudaMalloc((void**)&ctx->d_accum, npix * sizeof(float4));
+        cudaError_t e = rdc::dev_malloc((void**)&ctx->d_accum, npix * sizeof(float4));
         if (e != cudaSuccess) {
             ctx->has_scene = false;
             return cuda_fail(ctx, e, "cudaMalloc(accumulator)");
@@ -605,7 +639,7 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     }
     if (rdc_status st = ensure(ctx, &ctx->d_wf, &ctx->cap_wf, rdc::wavefront_state_bytes(npix), "wavefront state"))
         return st;
-    if (!ctx->d_wf_counts) RDC_CUDA(ctx, cudaMalloc((void**)&ctx->d_wf_counts, 8 * sizeof(uint32_t)));
+    if (!ctx->d_wf_counts) RDC_CUDA(ctx, rdc::dev_malloc((void**)&ctx->d_wf_counts, 8 * sizeof(uint32_t)));
     rdc::WfParams p;
     p.sc = ctx->view;
     p.accum = ctx->d_accum;
@@ -758,7 +792,7 @@ rdc_status fp32_probe(rdc_ctx* ctx, bool packed, double* best_out) {
     const int block = 256, blocks_per_sm = 8;  // 64 warps per SM
     const int grid = ctx->num_sms * blocks_per_sm;
     float* sink = nullptr;
-    RDC_CUDA(ctx, cudaMalloc((void**)&sink, grid * sizeof(float)));
+    RDC_CUDA(ctx, rdc::dev_malloc((void**)&sink, grid * sizeof(float)));
     int iters = 256;
     double best = 0.0;
     cudaError_t e = cudaSuccess;
@@ -820,7 +854,7 @@ rdc_status rdc_intersect_rays(rdc_ctx* ctx, const float* origins, const float* d
     const size_t f3 = (size_t)n * 3 * sizeof(float);
     char* buf = nullptr;
     const size_t total = 3 * f3 + n * sizeof(float) + n * sizeof(int32_t) + n;
-    RDC_CUDA(ctx, cudaMalloc((void**)&buf, total));
+    RDC_CUDA(ctx, rdc::dev_malloc((void**)&buf, total));
     float* d_o = (float*)buf;
     float* d_d = (float*)(buf + f3);
     float* d_n = (float*)(buf + 2 * f3);
@@ -858,7 +892,7 @@ rdc_status rdc_scatter_fixed(rdc_ctx* ctx, const float* origins, const float* di
     const size_t f3 = (size_t)n * 3 * sizeof(float);
     const size_t total = 4 * f3 + n * sizeof(float) + n * sizeof(int32_t) + (size_t)n * 12 * sizeof(uint32_t);
     char* buf = nullptr;
-    RDC_CUDA(ctx, cudaMalloc((void**)&buf, total));
+    RDC_CUDA(ctx, rdc::dev_malloc((void**)&buf, total));
     float* d_o = (float*)buf;
     float* d_d = (float*)(buf + f3);
     float* d_oo = (float*)(buf + 2 * f3);
@@ -1003,13 +1037,13 @@ rdc_status rdc_batch_upload(rdc_ctx* ctx, const rdc_batch_item* items, uint32_t 
         fast[i] = rdc::flatten(items[i].scene, rec.data() + rec_off[i], hit.data() + obj_off[i],
                                mat.data() + obj_off[i], runs.data() + run_off[i]);
 
-    cudaError_t e = cudaMalloc((void**)&b.d_rec, rec.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_hit, hit.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_mat, mat.size() * sizeof(MatDev));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_runs, runs.size() * sizeof(int4));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_accum, b.accum_total * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_pixel_counters, count * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_scenes, count * sizeof(rdc::BatchScene));
+    cudaError_t e = rdc::dev_malloc((void**)&b.d_rec, rec.size() * sizeof(float4));
+    if (e == cudaSuccess) e = rdc::dev_malloc((void**)&b.d_hit, hit.size() * sizeof(float4));
+    if (e == cudaSuccess) e = rdc::dev_malloc((void**)&b.d_mat, mat.size() * sizeof(MatDev));
+    if (e == cudaSuccess) e = rdc::dev_malloc((void**)&b.d_runs, runs.size() * sizeof(int4));
+    if (e == cudaSuccess) e = rdc::dev_malloc((void**)&b.d_accum, b.accum_total * sizeof(float4));
+    if (e == cudaSuccess) e = rdc::dev_malloc((void**)&b.d_pixel_counters, count * sizeof(uint32_t));
+    if (e == cudaSuccess) e = rdc::dev_malloc((void**)&b.d_scenes, count * sizeof(rdc::BatchScene));
     if (e != cudaSuccess) {
         free_batch(ctx);
         return cuda_fail(ctx, e, "rdc_batch_upload: cudaMalloc");

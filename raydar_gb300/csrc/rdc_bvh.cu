@@ -286,7 +286,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     // Device buffers: the 4-wide nodes + prims are kept; the rest (binary
     // nodes included) is build scratch.
     const size_t n_int = n >= 2 ? (size_t)n - 1 : 1;
-    cudaError_t e = cudaMalloc((void**)&out.prims, prims.size() * sizeof(float4));
+    cudaError_t e = dev_malloc((void**)&out.prims, prims.size() * sizeof(float4));
     size_t sort_tmp = 0, scan_tmp = 0;
     if (e == cudaSuccess)
         e = cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr,
@@ -300,7 +300,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     const size_t u32_b = (size_t)n * 4;
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t total = up(box_b) + up(bin_b) + 9 * up(u32_b) + up(256) + up(sort_tmp) + up(scan_tmp) + 256;
-    if (e == cudaSuccess) e = cudaMalloc((void**)&out.scratch, total);
+    if (e == cudaSuccess) e = dev_malloc((void**)&out.scratch, total);
     if (e != cudaSuccess) {
         out.release();
         return e;
@@ -361,7 +361,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
         out.nnodes = tail[0] + tail[1];
-        e = cudaMalloc((void**)&out.nodes, (size_t)out.nnodes * sizeof(Bvh4Node));
+        e = dev_malloc((void**)&out.nodes, (size_t)out.nnodes * sizeof(Bvh4Node));
         if (e != cudaSuccess) return e;
         collapse4_kernel<<<GI, B, 0, s>>>(bin, even, map, (int)n_int, out.nodes);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

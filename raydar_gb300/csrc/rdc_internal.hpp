@@ -122,6 +122,15 @@ cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, si
 // context: rdc_create, the .rscn reader/writer).
 void set_thread_error(const std::string& msg);
 
+// Every device allocation of the library (rdc_render_static makes none) goes
+// through dev_malloc.  Fault injection for tests, on the host: when
+// RDC_FAIL_ALLOC_AFTER=n is set in the environment at rdc_create, the
+// allocations after the next n fail with cudaErrorMemoryAllocation without
+// calling cudaMalloc (until the next rdc_create reads the variable again), so
+// every caller's out-of-memory path runs on a healthy GPU.
+cudaError_t dev_malloc(void** ptr, size_t bytes);
+void reset_alloc_injection();
+
 // Wavefront render (rdc_wavefront.cu): per-pixel path state as planes of
 // npix floats in one buffer of wavefront_state_bytes(npix).
 struct WfParams {

@@ -54,3 +54,26 @@ def test_batch_is_independent_of_launch_shape_and_replays():
     for i in range(len(items)):
         assert bits_equal(br.accumulator(i), first[i])
     br.close()
+
+
+def test_config3_batch_at_full_resolution_matches_the_oracle():
+    """The 64 seeded scenes of the batched workload (width 128..1024, 16:9 or
+    1:1, 4..12 bounces, 4..200 spheres + 0..20 cubes) at their full
+    resolution and bounce limit, with every scene's spp divided by 128 (at
+    least 1) so the oracle finishes in seconds, under the launch shape the
+    autotuner picks: each accumulator equals the oracle's render of that scene
+    (RNG stream = its batch index) bit for bit, and the segment counts add up."""
+    ws = scenegen.c3_batch()
+    items = [(w.scene, max(1, w.spp // 128), w.max_bounces, 3000 + i) for i, w in enumerate(ws)]
+    br = BatchRenderer(items)
+    tune = br.autotune()
+    br.render()
+    total = br.stats().segments
+    seg_sum = 0
+    for i, (sc, spp, bounces, seed) in enumerate(items):
+        ref, seg = oracle.render(sc.to_c(), 0, spp, bounces, seed, threads=16, stream=i)
+        assert bits_equal(br.accumulator(i), ref), f"scene {i} ({sc.width}x{sc.height}, {spp} spp)"
+        seg_sum += seg
+    assert total == seg_sum
+    assert tune["block_size"] in (64, 128, 256)
+    br.close()
