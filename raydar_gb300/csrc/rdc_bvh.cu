@@ -1,7 +1,8 @@
 // rdc_bvh.cu -- device build of the linear BVH used for large scenes.
 //
 //   1. object boxes and primitive records (host, exact reference constants)
-//   2. 30-bit Morton code of each box centre in the scene's centre bounds
+//   2. 30-bit Morton code of each box centre in the cube spanning the scene's
+//      centre bounds
 //   3. radix sort of (code, object) pairs (CUB)
 //   4. Karras, "Maximizing parallelism in the construction of BVHs, octrees
 //      and k-d trees" (HPG 2012): internal node i of N-1 finds its key range
@@ -11,9 +12,14 @@
 //      the second computes the union and continues.  No thread ever waits.
 //   6. tree depth (Karras trees over 30-bit codes with position tie-breaks
 //      are at most 63 deep)
-//   7. collapse to 4-wide nodes: the binary nodes at even depth, compacted
-//      by a prefix sum (CUB), each taking its grandchildren (or its leaf
-//      children) as children.
+//   7. collapse to 4-wide nodes, top down one level per launch: a 4-wide node
+//      starts from its binary node's two children and opens the internal
+//      child of largest surface area until it has four (a greedy surface-area
+//      collapse); nodes are numbered level by level through a prefix sum
+//      (CUB), so the layout is deterministic.  If that tree would be deeper
+//      than the traversal stack allows, the binary nodes at even depth are
+//      collapsed instead (each takes its grandchildren), which halves the
+//      depth.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -201,6 +207,92 @@ __global__ void collapse4_kernel(const BvhNode* __restrict__ bin, const uint32_t
     out[map[i]] = q;
 }
 
+// Greedy surface-area collapse.  The children of the 4-wide node of binary
+// node b: start from b's two children and open the internal child whose box
+// has the largest surface area (lowest slot on ties) until there are four or
+// only leaves are left.  Returns the count; ids are binary node indices (>= 0)
+// or ~object.
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ int greedy_children(const BvhNode* __restrict__ bin, int b, int id[4], float4 lo[4],
+                                               float4 hi[4]) {
+    const BvhNode nd = bin[b];
+    id[0] = __float_as_int(nd.a.w);
+    lo[0] = nd.a;
+    hi[0] = nd.b;
+    id[1] = __float_as_int(nd.b.w);
+    lo[1] = nd.c;
+    hi[1] = nd.d;
+    int k = 2;
+    while (k < 4) {
+        int best = -1;
+        float ba = -1.0f;
+        for (int j = 0; j < k; ++j) {
+            if (id[j] < 0) continue;
+            const float a = half_area(lo[j], hi[j]);
+            if (a > ba) {
+                ba = a;
+                best = j;
+            }
+        }
+        if (best < 0) break;
+        const BvhNode m = bin[id[best]];
+        id[best] = __float_as_int(m.a.w);
+        lo[best] = m.a;
+        hi[best] = m.b;
+        id[k] = __float_as_int(m.b.w);
+        lo[k] = m.c;
+        hi[k] = m.d;
+        ++k;
+    }
+    return k;
+}
+
+// Level pass 1: the number of internal children of each frontier node.
+__global__ void collapse_count_kernel(const BvhNode* __restrict__ bin, const int2* __restrict__ front, uint32_t m,
+                                      uint32_t* __restrict__ count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    int id[4];
+    float4 lo[4], hi[4];
+    const int k = greedy_children(bin, front[i].x, id, lo, hi);
+    uint32_t c = 0;
+    for (int j = 0; j < k; ++j) c += id[j] >= 0 ? 1u : 0u;
+    count[i] = c;
+}
+
+// Level pass 2: write frontier node i's 4-wide node at front[i].y; its
+// internal children become nodes next_base + off[i] + r (r their rank in
+// slot order) and the next level's frontier entries off[i] + r.
+__global__ void collapse_write_kernel(const BvhNode* __restrict__ bin, const int2* __restrict__ front, uint32_t m,
+                                      const uint32_t* __restrict__ off, uint32_t next_base, Bvh4Node* out,
+                                      int2* __restrict__ next) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    int id[4];
+    float4 lo[4], hi[4];
+    const int k = greedy_children(bin, front[i].x, id, lo, hi);
+    Bvh4Node q;
+    uint32_t r = off[i];
+    for (int j = 0; j < k; ++j) {
+        if (id[j] < 0) {
+            put4(q, j, lo[j], hi[j], id[j]);
+        } else {
+            const int idx = (int)(next_base + r);
+            put4(q, j, lo[j], hi[j], idx);
+            next[r] = make_int2(id[j], idx);
+            ++r;
+        }
+    }
+    const float INF = __int_as_float(0x7f800000);
+    const float4 empty = make_float4(INF, INF, INF, 0.0f);
+    for (int j = k; j < 4; ++j) put4(q, j, empty, empty, 0);
+    out[front[i].y] = q;
+}
+
 }  // namespace
 
 void BvhDevice::release() {
@@ -294,12 +386,14 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     if (e == cudaSuccess)
         e = cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n_int, s);
     // scratch: box (2n float4) | binary nodes (n-1) | keys, keys2, vals, vals2 (4n u32) | parents (2n int) |
-    //          flags, even, map (3n u32) | depth | sort tmp | scan tmp
+    //          flags, even, map (3n u32) | two collapse frontiers (n-1 int2 each) | depth | sort tmp | scan tmp
     const size_t box_b = 2 * (size_t)n * sizeof(float4);
     const size_t bin_b = n_int * sizeof(BvhNode);
     const size_t u32_b = (size_t)n * 4;
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t total = up(box_b) + up(bin_b) + 9 * up(u32_b) + up(256) + up(sort_tmp) + up(scan_tmp) + 256;
+    const size_t front_b = n_int * sizeof(int2);
+    const size_t total =
+        up(box_b) + up(bin_b) + 9 * up(u32_b) + 2 * up(front_b) + up(256) + up(sort_tmp) + up(scan_tmp) + 256;
     if (e == cudaSuccess) e = dev_malloc((void**)&out.scratch, total);
     if (e != cudaSuccess) {
         out.release();
@@ -323,6 +417,8 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     uint32_t* flags = (uint32_t*)take(u32_b);
     uint32_t* even = (uint32_t*)take(u32_b);
     uint32_t* map = (uint32_t*)take(u32_b);
+    int2* front = (int2*)take(front_b);
+    int2* front_next = (int2*)take(front_b);
     uint32_t* d_depth = (uint32_t*)take(256);
     void* d_sort = take(sort_tmp);
     void* d_scan = take(scan_tmp);
@@ -335,7 +431,13 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     if (e != cudaSuccess) return e;
     const float3 lo = make_float3(clo[0], clo[1], clo[2]);
     auto inv = [](float a, float b) { return b > a ? 1.0f / (b - a) : 0.0f; };
-    const float3 inv_ext = make_float3(inv(clo[0], chi[0]), inv(clo[1], chi[1]), inv(clo[2], chi[2]));
+    // One scale for all axes (the largest extent): per-axis scaling would split
+    // a flat domain's short axis as often as its long ones, giving flat boxes
+    // of large surface area (config 5's 40 x 10 x 40 box: 19.8 -> 18.5 node
+    // visits per segment, +6%).
+    const float ext = std::max(chi[0] - clo[0], std::max(chi[1] - clo[1], chi[2] - clo[2]));
+    const float ie = inv(0.0f, ext);
+    const float3 inv_ext = make_float3(ie, ie, ie);
     const uint32_t B = 256, G = (n + B - 1) / B;
     morton_kernel<<<G, B, 0, s>>>(d_box, n, lo, inv_ext, keys, vals);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -350,6 +452,47 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         depth_kernel<<<G, B, 0, s>>>(parent_node, parent_leaf, (int)n, d_depth);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+
+        // Greedy surface-area collapse, one level per pass (count, scan,
+        // write).  At most n - 1 4-wide nodes (each holds >= 2 children).
+        e = dev_malloc((void**)&out.nodes, n_int * sizeof(Bvh4Node));
+        if (e != cudaSuccess) return e;
+        const int2 root = make_int2(0, 0);
+        e = cudaMemcpyAsync(front, &root, sizeof(int2), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        uint32_t m = 1, total = 1, levels = 0;
+        while (m > 0 && levels <= 32) {
+            ++levels;
+            const uint32_t GM = (m + B - 1) / B;
+            collapse_count_kernel<<<GM, B, 0, s>>>(bin, front, m, even);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, even, map, (int)m, s);
+            if (e != cudaSuccess) return e;
+            collapse_write_kernel<<<GM, B, 0, s>>>(bin, front, m, map, total, out.nodes, front_next);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            uint32_t tl[2] = {0, 0};
+            e = cudaMemcpyAsync(&tl[0], map + m - 1, 4, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&tl[1], even + m - 1, 4, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            m = tl[0] + tl[1];
+            total += m;
+            std::swap(front, front_next);
+        }
+        if (m == 0) {
+            out.nnodes = total;
+            e = cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            if (depth_out) *depth_out = depth;
+            cudaFree(out.scratch);
+            out.scratch = nullptr;
+            out.scratch_bytes = 0;
+            return cudaSuccess;
+        }
+        // Deeper than 32 levels (3 stack entries each): the even-depth collapse.
+        cudaFree(out.nodes);
+        out.nodes = nullptr;
         even_depth_kernel<<<GI, B, 0, s>>>(parent_node, (int)n_int, even);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, even, map, (int)n_int, s);
