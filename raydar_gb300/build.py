@@ -2,6 +2,11 @@
 
 Everything is built in-tree (outputs are git-ignored):
   raydar_gb300/libraydar_cuda.so     the product: kernels + the C ABI of include/raydar_cuda.h
+  raydar_gb300/libraydar_cuda_checked.so
+                                     the same sources with device bounds checks
+                                     (-DRDC_BOUNDS_CHECK=1: out-of-range indices are counted and
+                                     reported as RDC_ERR_DEVICE, never trap); built on demand by
+                                     its test, the stand-in for a memory checker
   oracle/_build/liboracle_raydar.so  test infrastructure: the CPU restatement of the reference
   raydar_gb300/_build/*.o            intermediate objects and the ptxas resource report
 
@@ -22,6 +27,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
 LIB = PKG / "libraydar_cuda.so"
+LIB_CHECKED = PKG / "libraydar_cuda_checked.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "liboracle_raydar.so"
 
@@ -60,36 +66,41 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build_library(force: bool = False, verbose: bool = False) -> Path:
-    """Compile csrc/*.cu and csrc/*.cpp for sm_103a and link libraydar_cuda.so."""
-    BUILD.mkdir(exist_ok=True)
+def build_library(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile csrc/*.cu and csrc/*.cpp for sm_103a and link libraydar_cuda.so
+    (checked: the bounds-checked libraydar_cuda_checked.so)."""
+    build_dir = PKG / "_build_checked" if checked else BUILD
+    lib = LIB_CHECKED if checked else LIB
+    extra = ["-DRDC_BOUNDS_CHECK=1"] if checked else []
+    build_dir.mkdir(exist_ok=True)
     nvcc = _nvcc()
     headers = list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     incs = ["-I", str(INCLUDE), "-I", str(CSRC)]
     jobs = []
     objs = []
     for src in sorted(CSRC.glob("*.cu")):
-        obj = BUILD / (src.stem + ".cu.o")
+        obj = build_dir / (src.stem + ".cu.o")
         objs.append(obj)
         if force or _stale(obj, [src, *headers]):
-            jobs.append(([nvcc, *ARCH, *NVCC_DEVICE, *incs, "-c", str(src), "-o", str(obj)],
-                         BUILD / (src.stem + ".ptxas.txt")))
+            jobs.append(([nvcc, *ARCH, *NVCC_DEVICE, *extra, *incs, "-c", str(src), "-o", str(obj)],
+                         build_dir / (src.stem + ".ptxas.txt")))
     cxx = os.environ.get("CXX", "g++")
     for src in sorted(CSRC.glob("*.cpp")):
-        obj = BUILD / (src.stem + ".cpp.o")
+        obj = build_dir / (src.stem + ".cpp.o")
         objs.append(obj)
         if force or _stale(obj, [src, *headers]):
-            jobs.append(([cxx, *HOST_CXX, *incs, "-I", _cuda_include(), "-c", str(src), "-o", str(obj)], None))
+            jobs.append(([cxx, *HOST_CXX, *extra, *incs, "-I", _cuda_include(), "-c", str(src), "-o", str(obj)],
+                         None))
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for fut in [ex.submit(_run, cmd, log) for cmd, log in jobs]:
             fut.result()
-    if force or jobs or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fPIC",
+    if force or jobs or _stale(lib, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-Xcompiler", "-fPIC",
               "-lpthread", "-ldl", "-lrt"])
     if verbose:
-        for f in sorted(BUILD.glob("*.ptxas.txt")):
+        for f in sorted(build_dir.glob("*.ptxas.txt")):
             sys.stdout.write(f.read_text())
-    return LIB
+    return lib
 
 
 def build_oracle(force: bool = False) -> Path:

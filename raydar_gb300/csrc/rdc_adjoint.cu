@@ -77,7 +77,7 @@ __device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& 
                                             float wk, V3& go, V3& gd) {
     const int obj = (int)(v.objf & 0xFFFFFFu);
     const uint32_t f = v.objf >> 24;
-    const float4 hi = __ldg(&sc.hit[obj]);
+    const float4 hi = __ldg(&sc.hit[checked_index(sc.oob, obj, sc.nobj)]);
     const int kind = __float_as_int(m.d.y);
     const HitRec h = closest_hit(v.o, v.d, v.t, hi, kind);
     const float r = m.a.w;
@@ -206,7 +206,7 @@ __device__ __forceinline__ float vertex_vjp(const SceneView& sc, const AdjVert& 
 // the sums at g + 8 * obj with one atomic per object and component: the
 // lanes sharing an object form a list in lane order, and pointer jumping
 // (5 rounds) leaves the list's total with its first lane.
-__device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7]) {
+__device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7], unsigned long long* oob, uint32_t nobj) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(FULL, obj);
@@ -228,7 +228,7 @@ __device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7]) {
         }
     }
     if (obj >= 0 && lane == __ffs(peers) - 1) {
-        float* dst = g + 8 * (size_t)obj;
+        float* dst = g + 8 * (size_t)checked_index(oob, obj, nobj);
 #pragma unroll
         for (int j = 0; j < 7; ++j)
             if (c[j] != 0.0f) atomicAdd(dst + j, c[j]);
@@ -273,8 +273,8 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
             const uint32_t pix = (uint32_t)(path / P.nspp);
             const uint32_t sample = P.s0 + (uint32_t)(path % P.nspp);
             const float inv_n = 1.0f / (float)P.nspp;
-            gw = mk(P.dl[3 * (size_t)pix] * inv_n, P.dl[3 * (size_t)pix + 1] * inv_n,
-                    P.dl[3 * (size_t)pix + 2] * inv_n);
+            const size_t px3 = 3 * (size_t)checked_index(P.sc.oob, pix, (long long)P.sc.width * P.sc.height);
+            gw = mk(P.dl[px3] * inv_n, P.dl[px3 + 1] * inv_n, P.dl[px3 + 2] * inv_n);
             if (gw.x != 0.0f || gw.y != 0.0f || gw.z != 0.0f) {
                 // replay (the forward kernels' arithmetic, bit for bit)
                 V3 o, d;
@@ -295,6 +295,7 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
                         missed = true;
                         break;
                     }
+                    idx = (int)checked_index(P.sc.oob, idx, P.sc.nobj);
                     const MatDev m = load_mat(P.sc.mat, idx);
                     const HitRec h = closest_hit(o, d, t, __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
                     uint32_t w[12];
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
                 for (int k = sweep ? nv - 1 : -1; k >= 0; --k) {
                     AdjVert& vk = v[k];
                     const int obj = (int)(vk.objf & 0xFFFFFFu);
-                    const MatDev m = load_mat(P.sc.mat, obj);
+                    const MatDev m = load_mat(P.sc.mat, (int)checked_index(P.sc.oob, obj, P.sc.nobj));
                     const V3 s = vk.s;
                     const float wk = gw.x * S.x + gw.y * S.y + gw.z * S.z;
                     const float gr = vertex_vjp(P.sc, vk, m, s, wk, go, gd);
@@ -377,10 +378,10 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
             c[5] = has ? gw.z : 0.0f;
             c[6] = has ? v[k].t : 0.0f;
             if (has) {
-                const float4 alb = __ldg(&P.sc.mat[obj].a);
+                const float4 alb = __ldg(&P.sc.mat[checked_index(P.sc.oob, obj, P.sc.nobj)].a);
                 pre = mk(pre.x * alb.x, pre.y * alb.y, pre.z * alb.z);
             }
-            warp_add_grad(gbase, obj, c);
+            warp_add_grad(gbase, obj, c, P.sc.oob, P.sc.nobj);
         }
     }
     // flush the block's shared accumulators; counters

@@ -24,6 +24,7 @@ using rdc::MatDev;
 constexpr size_t kMaxSceneSmem = 200 * 1024;
 constexpr size_t kCounters = 8;       // device counters per context
 constexpr size_t kErrorCounter = 4;   // index of the device-error count
+constexpr size_t kBoundsCounter = 5;  // out-of-range indices caught (bounds-checked build)
 
 struct rdc_ctx {
     int device = 0;
@@ -147,13 +148,17 @@ rdc_status set_device(rdc_ctx* ctx) {
 // (a bulk copy whose completion they stopped waiting for, rdc_device.cuh);
 // after a synchronisation the count is reported once as RDC_ERR_DEVICE.
 rdc_status check_device_errors(rdc_ctx* ctx) {
-    unsigned long long n = 0;
-    RDC_CUDA(ctx, cudaMemcpy(&n, ctx->d_counters + kErrorCounter, sizeof(n), cudaMemcpyDeviceToHost));
-    if (n == 0) return RDC_OK;
+    static_assert(kBoundsCounter == kErrorCounter + 1, "the two device-error counters are adjacent");
+    unsigned long long n[2] = {0, 0};
+    RDC_CUDA(ctx, cudaMemcpy(n, ctx->d_counters + kErrorCounter, sizeof(n), cudaMemcpyDeviceToHost));
+    if (n[0] == 0 && n[1] == 0) return RDC_OK;
     RDC_CUDA(ctx, cudaMemset(ctx->d_counters + kErrorCounter, 0, sizeof(n)));
+    if (n[1] != 0)
+        return fail(ctx, RDC_ERR_DEVICE,
+                    std::to_string(n[1]) + " out-of-range device index(es) caught by the bounds-checked build");
     return fail(ctx, RDC_ERR_DEVICE,
-                std::to_string(n) + " block(s) could not stage the scene into shared memory (bulk copy did not "
-                                    "complete); their pixels were not rendered");
+                std::to_string(n[0]) + " block(s) could not stage the scene into shared memory (bulk copy did not "
+                                       "complete); their pixels were not rendered");
 }
 
 // Checks shared by every scene entry point.  The reference accepts any
@@ -181,8 +186,9 @@ rdc_status check_scene(rdc_ctx* ctx, const rdc_scene_desc* sc, const std::string
 }
 
 void fill_view(rdc::SceneView& v, const rdc_scene_desc* sc, const float4* rec, uint32_t nrec, const float4* hit,
-               const MatDev* mat, const int4* runs, uint32_t nruns, bool fast_div) {
+               const MatDev* mat, const int4* runs, uint32_t nruns, bool fast_div, unsigned long long* oob) {
     const rdc_camera& cam = sc->camera;
+    v.oob = oob;
     v.rec = rec;
     v.nrec = nrec;
     v.hit = hit;
@@ -412,7 +418,8 @@ rdc_status rdc_scene_upload(rdc_ctx* ctx, const rdc_scene_desc* sc) {
     // Host staging vectors die at return: wait for the copies.
     RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
-    fill_view(ctx->view, sc, ctx->d_rec, fc.nrec, ctx->d_hit, ctx->d_mat, ctx->d_runs, fc.nruns, fast_div);
+    fill_view(ctx->view, sc, ctx->d_rec, fc.nrec, ctx->d_hit, ctx->d_mat, ctx->d_runs, fc.nruns, fast_div,
+              ctx->d_counters + kBoundsCounter);
     ctx->brute_fits = brute_fits;
     ctx->has_scene = false;
     ctx->host_objects.assign(sc->objects, sc->objects + n);
@@ -520,7 +527,7 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
         return fail(ctx, RDC_ERR_LIMIT,
                     "rdc_render: brute force needs the scene's records in shared memory (at most "
                     "RDC_MAX_BRUTE_OBJECTS objects); use RDC_ACCEL_LBVH or RDC_ACCEL_AUTO");
-    p.bvh = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
+    p.bvh = ctx->bvh_active ? ctx->bvh.view(ctx->d_counters + kBoundsCounter) : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f, 0, nullptr};
     p.bvh_counters = ctx->d_counters + 2;
     p.min_idle = ctx->render_cfg.refill_min_idle;
     const int block = (int)ctx->render_cfg.block_size;
@@ -735,7 +742,7 @@ rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo
     if (nobj > 0 && npix > 0) {
         rdc::AdjParams p;
         p.sc = ctx->view;
-        p.bvh = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
+        p.bvh = ctx->bvh_active ? ctx->bvh.view(ctx->d_counters + kBoundsCounter) : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f, 0, nullptr};
         p.dl = ctx->d_dl;
         p.grad = ctx->d_grad;
         p.s0 = ctx->adj_s0;
@@ -863,7 +870,7 @@ rdc_status rdc_intersect_rays(rdc_ctx* ctx, const float* origins, const float* d
     uint8_t* d_f = (uint8_t*)(buf + 3 * f3 + n * sizeof(float) + n * sizeof(int32_t));
     cudaError_t e = cudaMemcpyAsync(d_o, origins, f3, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, directions, f3, cudaMemcpyHostToDevice, ctx->stream);
-    const rdc::BvhView bv = ctx->bvh_active ? ctx->bvh.view() : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f};
+    const rdc::BvhView bv = ctx->bvh_active ? ctx->bvh.view(ctx->d_counters + kBoundsCounter) : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f, 0, nullptr};
     if (e == cudaSuccess)
         e = rdc::launch_intersect_rays(ctx->view, bv, d_o, d_d, n, d_t, d_i, d_n, d_f, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, d_t, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
@@ -1053,7 +1060,7 @@ rdc_status rdc_batch_upload(rdc_ctx* ctx, const rdc_batch_item* items, uint32_t 
     for (uint32_t i = 0; i < count; ++i) {
         rdc::BatchScene& bs = scenes[i];
         fill_view(bs.sc, items[i].scene, b.d_rec + rec_off[i], fc[i].nrec, b.d_hit + obj_off[i],
-                  b.d_mat + obj_off[i], b.d_runs + run_off[i], fc[i].nruns, fast[i] != 0);
+                  b.d_mat + obj_off[i], b.d_runs + run_off[i], fc[i].nruns, fast[i] != 0, ctx->d_counters + kBoundsCounter);
         bs.accum = b.d_accum + b.accum_off[i];
         bs.npix = b.width[i] * b.height[i];
         bs.spp = items[i].spp;

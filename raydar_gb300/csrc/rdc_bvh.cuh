@@ -91,7 +91,7 @@ __device__ __forceinline__ void bvh_sphere_leaf(const RayPre& r, float4 p0, floa
 template <bool Fast>
 __device__ __forceinline__ void bvh_leaf(const BvhView& bv, const RayPre& r, int obj, float& best, int& bidx) {
     float4 p0, p1;
-    ldg_pair(bv.prims + 2 * obj, p0, p1);
+    ldg_pair(bv.prims + 2 * checked_index(bv.oob, obj, bv.nobj), p0, p1);
     if (__float_as_int(p1.w) == RDC_GEOMETRY_SPHERE) {
         bvh_sphere_leaf<Fast>(r, p0, p1.x, obj, best, bidx);
     } else {
@@ -229,7 +229,7 @@ __device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb
 template <class Stack>
 __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T, Stack& stack,
                                          BvhCounters& cnt) {
-    const float4* np = bv.nodes[T.cur].v;
+    const float4* np = bv.nodes[checked_index(bv.oob, T.cur, bv.nnodes)].v;
     float4 lo[4], hi[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) ldg_pair(np + 2 * j, lo[j], hi[j]);
@@ -285,7 +285,7 @@ __device__ __forceinline__ void bvh_leaf_step(const BvhView& bv, const RayPre& r
                                               BvhCounters& cnt) {
     const int j = __ffs(T.lmask) - 1;
     T.lmask &= T.lmask - 1u;
-    const int child = __float_as_int(__ldg(&bv.nodes[T.lnode].v[2 * j].w));
+    const int child = __float_as_int(__ldg(&bv.nodes[checked_index(bv.oob, T.lnode, bv.nnodes)].v[2 * j].w));
     ++cnt.tests;
     bvh_leaf_any(bv, r, fast, ~child, T.best, T.bidx);
 }

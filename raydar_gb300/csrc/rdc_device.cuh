@@ -45,6 +45,28 @@ __device__ __forceinline__ U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint
     return U4{c0, c1, c2, c3};
 }
 
+// Bounds-checked build (-DRDC_BOUNDS_CHECK=1, libraydar_cuda_checked.so): the
+// stand-in for a memory checker.  Every data-dependent index into a device
+// array goes through checked_index, which counts an index outside [0, n) in
+// *oob and substitutes 0 (every such array has at least one element), so a
+// stray index is reported (RDC_ERR_DEVICE at the next synchronisation)
+// instead of faulting, and never traps.  The normal build compiles it away.
+#ifndef RDC_BOUNDS_CHECK
+#define RDC_BOUNDS_CHECK 0
+#endif
+
+__device__ __forceinline__ long long checked_index(unsigned long long* oob, long long i, long long n) {
+#if RDC_BOUNDS_CHECK
+    if (i >= 0 && i < n) return i;
+    atomicAdd(oob, 1ull);
+    return 0;
+#else
+    (void)oob;
+    (void)n;
+    return i;
+#endif
+}
+
 // rand 0.8.5 Standard f32: top 24 bits * 2^-24 in [0, 1).
 __device__ __forceinline__ float u01(uint32_t u) {
     return __fmul_rn(__uint2float_rn(u >> 8), 5.9604644775390625e-8f);
@@ -837,8 +859,9 @@ __device__ __forceinline__ bool segment_shade(const SceneView& sc, PathState& s,
         s.light = vadd(s.light, mk(sky.x * s.atten.x, sky.y * s.atten.y, sky.z * s.atten.z));
         return true;
     }
-    const float4 hi = __ldg(&sc.hit[idx]);
-    const MatDev m = load_mat(sc.mat, idx);
+    const int ci = (int)checked_index(sc.oob, idx, sc.nobj);
+    const float4 hi = __ldg(&sc.hit[ci]);
+    const MatDev m = load_mat(sc.mat, ci);
     const HitRec h = closest_hit(s.o, s.d, t, hi, __float_as_int(m.d.y));
     uint32_t w[12];
     const uint32_t c2 = s.bounce * 4u;

@@ -50,6 +50,7 @@ struct SceneView {
     float top[3];
     float bottom[3];
     float solid[3];
+    unsigned long long* oob;  // bounds-checked build: count of out-of-range indices caught
 };
 
 struct Bvh4Node;  // rdc_bvh.cuh
@@ -62,6 +63,8 @@ struct BvhView {
     uint32_t nobj;
     float scene_r;  // bound on |centre| + size over the objects
     float o_max;    // sphere leaf boxes are grown for ray origins with |o| <= o_max
+    uint32_t nnodes;
+    unsigned long long* oob;  // bounds-checked build: count of out-of-range indices caught
 };
 
 struct BvhDevice {
@@ -74,7 +77,7 @@ struct BvhDevice {
     float scene_r = 0.0f;
     float o_max = 0.0f;
     void release();
-    BvhView view() const { return BvhView{nodes, prims, nobj, scene_r, o_max}; }
+    BvhView view(unsigned long long* oob) const { return BvhView{nodes, prims, nobj, scene_r, o_max, nnodes, oob}; }
 };
 
 // Build the LBVH of `sc` on stream `s` (synchronises it).  depth_out: the

@@ -47,7 +47,7 @@ __device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& is
                 const unsigned mine = base + __popc(need & ((1u << lane) - 1u));
                 if (mine < P.npix) {
                     pix = (int)mine;
-                    acc = P.accum[pix];
+                    acc = P.accum[checked_index(P.sc.oob, pix, P.npix)];
                     path_start(P.sc, mine, st);
                     path_keep(st, pdir);
                     sample = P.s0;
@@ -66,7 +66,7 @@ __device__ __forceinline__ uint32_t render_loop(const RenderParams& P, Isect& is
             acc.w = acc.w + 1.0f;
             ++sample;
             if (sample == send) {
-                P.accum[pix] = acc;
+                P.accum[checked_index(P.sc.oob, pix, P.npix)] = acc;
                 pix = -1;
             } else {
                 path_restart(P.sc, pdir, st);  // next sample of the same pixel
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
                 acc.w = acc.w + 1.0f;
                 ++sample;
                 if (sample == send) {
-                    P.accum[pix] = acc;
+                    P.accum[checked_index(P.sc.oob, pix, P.npix)] = acc;
                     pix = -1;
                     in_flight = false;
                     return;
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kRenderBlock, 2) render_bvh_kernel(const Rende
                 const unsigned mine = base + __popc(need & ((1u << lane) - 1u));
                 if (mine < P.npix) {
                     pix = (int)mine;
-                    acc = P.accum[pix];
+                    acc = P.accum[checked_index(P.sc.oob, pix, P.npix)];
                     path_start(P.sc, mine, st);
                     path_keep(st, pdir);
                     sample = P.s0;
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kRenderBlock, 3) batch_kernel(const BatchParam
                     const unsigned mine = base + __popc(need & ((1u << lane) - 1u));
                     if (mine < npix) {
                         pix = (int)mine;
-                        acc = s_bs.accum[pix];
+                        acc = s_bs.accum[checked_index(s_bs.sc.oob, pix, s_bs.npix)];
                         path_start(s_bs.sc, mine, st);
                         path_keep(st, pdir);
                         sample = 0;
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(kRenderBlock, 3) batch_kernel(const BatchParam
                 acc.w = acc.w + 1.0f;
                 ++sample;
                 if (sample == s_bs.spp) {
-                    s_bs.accum[pix] = acc;
+                    s_bs.accum[checked_index(s_bs.sc.oob, pix, s_bs.npix)] = acc;
                     pix = -1;
                 } else {
                     path_restart(s_bs.sc, pdir, st);
@@ -400,8 +400,9 @@ __global__ void intersect_rays_kernel(const SceneView sc, const BvhView bvh, con
     }
     idx_out[i] = idx;
     if (idx >= 0) {
-        const MatDev m = load_mat(sc.mat, idx);
-        const HitRec h = closest_hit(ro, rd, t, sc.hit[idx], __float_as_int(m.d.y));
+        const int ci = (int)checked_index(sc.oob, idx, sc.nobj);
+        const MatDev m = load_mat(sc.mat, ci);
+        const HitRec h = closest_hit(ro, rd, t, sc.hit[ci], __float_as_int(m.d.y));
         t_out[i] = t;
         n_out[3 * i] = h.n.x;
         n_out[3 * i + 1] = h.n.y;

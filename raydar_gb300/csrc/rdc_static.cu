@@ -210,6 +210,7 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
         v.nruns = fc.nruns;
         v.fast_div = fast_div ? 1u : 0u;
         v.neg_zero = make_float2(-0.0f, -0.0f);
+        v.oob = d_counters + 4;  // reported with the device-error count
         v.width = cam.resolution_x;
         v.height = cam.resolution_y;
         for (int i = 0; i < 3; ++i) v.cam_pos[i] = cam.position[i];

@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
         int cls = -1;
         uint32_t pix = 0;
         if (k < n) {
-            pix = q_in[k];
+            pix = (uint32_t)checked_index(P.sc.oob, q_in[k], P.npix);
             const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
             const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
             const RayPre r = ray_pre(o, d, P.sc.neg_zero);
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
             P.hit_t[pix] = t;
             P.hit_obj[pix] = idx;
             ++segs;
-            cls = idx < 0 ? 3 : material_class(P.sc.mat[idx]);
+            cls = idx < 0 ? 3 : material_class(P.sc.mat[checked_index(P.sc.oob, idx, P.sc.nobj)]);
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
             uint32_t b = 0;
             if (lane == leader) b = atomicAdd(&P.counts[2 + c], (uint32_t)__popc(m));
             b = __shfl_sync(FULL, b, leader);
-            if (cls == c) P.cls[(size_t)c * P.npix + b + __popc(m & ((1u << lane) - 1u))] = pix;
+            if (cls == c)
+                P.cls[(size_t)c * P.npix + checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npix)] = pix;
         }
     }
     unsigned long long s = segs;
@@ -116,7 +117,8 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
         if (k < total) {
             const int c = k < e0 ? 0 : (k < e1 ? 1 : (k < e2 ? 2 : 3));
             const uint32_t pos = k - (c == 0 ? 0u : (c == 1 ? e0 : (c == 2 ? e1 : e2)));
-            pix = P.cls[(size_t)c * P.npix + pos];
+            pix = (uint32_t)checked_index(P.sc.oob, P.cls[(size_t)c * P.npix + checked_index(P.sc.oob, pos, P.npix)],
+                                          P.npix);
             const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
             V3 atten = mk(P.ar[pix], P.ag[pix], P.ab[pix]);
             V3 light = mk(P.lr[pix], P.lg[pix], P.lb[pix]);
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
                 light = vadd(light, mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z));
             } else {
                 const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
-                const int idx = P.hit_obj[pix];
+                const int idx = (int)checked_index(P.sc.oob, P.hit_obj[pix], P.sc.nobj);
                 const MatDev m = load_mat(P.sc.mat, idx);
                 const HitRec h = closest_hit(o, d, P.hit_t[pix], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
                 uint32_t w[12];
@@ -154,7 +156,7 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
             uint32_t b = 0;
             if (lane == leader) b = atomicAdd(n_out, (uint32_t)__popc(m));
             b = __shfl_sync(FULL, b, leader);
-            if (requeue) q_out[b + __popc(m & ((1u << lane) - 1u))] = pix;
+            if (requeue) q_out[checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npix)] = pix;
         }
     }
 }
