@@ -353,7 +353,9 @@ rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo
                         float* grad_emission);
 
 /* Set / get the launch shape of rdc_render.  block_size and blocks_per_sm as
- * for a batch (default 256, 0).  refill_min_idle applies to LBVH renders: a
+ * for a batch (default 256, 0); LBVH renders use blocks of at most 128
+ * threads (their kernel is compiled for 5 such blocks per SM).
+ * refill_min_idle applies to LBVH renders: a
  * warp keeps stepping its lanes' traversals until this many have finished,
  * then shades those together (default 16).  Brute-force renders refill each
  * idle lane at once.  Affects results never, speed only. */

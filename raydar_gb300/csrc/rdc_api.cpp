@@ -244,7 +244,7 @@ rdc_status apply_accel(rdc_ctx* ctx, bool scene_changed) {
     if (depth > 64) {
         ctx->bvh.release();
         ctx->bvh_active = false;
-        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the traversal stack allows (3 entries per 4-wide level)");
+        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the traversal stack allows (width - 1 entries per wide level)");
     }
     ctx->bvh_active = n > 0;
     ctx->bvh_depth = depth;
@@ -530,7 +530,8 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
     p.bvh = ctx->bvh_active ? ctx->bvh.view(ctx->d_counters + kBoundsCounter) : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f, 0, nullptr};
     p.bvh_counters = ctx->d_counters + 2;
     p.min_idle = ctx->render_cfg.refill_min_idle;
-    const int block = (int)ctx->render_cfg.block_size;
+    const int block = ctx->bvh_active ? std::min<int>((int)ctx->render_cfg.block_size, rdc::kRenderBvhBlock)
+                                      : (int)ctx->render_cfg.block_size;
     const size_t smem = ctx->bvh_active ? 0 : rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
     int per_sm = 0;
     if (ctx->bvh_active)

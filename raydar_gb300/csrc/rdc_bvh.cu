@@ -16,14 +16,15 @@
 //   6b. tree depth (Karras trees over 30-bit codes with position tie-breaks
 //      are at most 63 deep; a restructured tree deeper than 62 is rebuilt
 //      without restructuring)
-//   7. collapse to 4-wide nodes, top down one level per launch: a 4-wide node
-//      starts from its binary node's two children and opens the internal
-//      child of largest surface area until it has four (a greedy surface-area
-//      collapse); nodes are numbered level by level through a prefix sum
-//      (CUB), so the layout is deterministic.  If that tree would be deeper
-//      than the traversal stack allows, the binary nodes at even depth are
-//      collapsed instead (each takes its grandchildren), which halves the
-//      depth.
+//   7. collapse to wide nodes (kBvhWidth children), top down one level per
+//      pass: a wide node starts from its binary node's two children and opens
+//      the internal child of largest surface area until it is full (a greedy
+//      surface-area collapse); nodes are numbered level by level through a prefix sum
+//      (CUB), so the layout is deterministic and every node's internal
+//      children have consecutive indices.  If that tree would be deeper than
+//      the traversal stack allows, every internal child is opened a fixed
+//      number of times instead (each node takes the binary nodes 2 or 3
+//      levels below its own), which divides the depth by that many.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -321,67 +322,24 @@ __global__ void restructure_kernel(const int* __restrict__ parent_leaf_start, in
     }
 }
 
-// even[i] = 1 when internal node i is at even depth (the root is at 0):
-// those nodes become the 4-wide tree.
-__global__ void even_depth_kernel(const int* __restrict__ parent_node, int n_internal, uint32_t* even) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_internal) return;
-    uint32_t depth = 0;
-    int p = parent_node[i];
-    while (p >= 0 && depth < 200) {
-        ++depth;
-        p = parent_node[p >> 1];
-    }
-    even[i] = (depth & 1u) ? 0u : 1u;
-}
-
-__device__ __forceinline__ void put4(Bvh4Node& q, int j, float4 lo, float4 hi, int child) {
-    q.v[2 * j] = make_float4(lo.x, lo.y, lo.z, __int_as_float(child));
-    q.v[2 * j + 1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
-}
-
-// The 4-wide node of even-depth binary node i: its leaf children and the
-// children of its internal children (all at even depth again), at the
-// compacted index map[i] (exclusive prefix sum of even[]).
-__global__ void collapse4_kernel(const BvhNode* __restrict__ bin, const uint32_t* __restrict__ even,
-                                 const uint32_t* __restrict__ map, int n_internal, Bvh4Node* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_internal || !even[i]) return;
-    Bvh4Node q;
-    int k = 0;
-    const BvhNode nd = bin[i];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const int c = __float_as_int(s ? nd.b.w : nd.a.w);
-        if (c < 0) {
-            put4(q, k++, s ? nd.c : nd.a, s ? nd.d : nd.b, c);
-        } else {
-            const BvhNode m = bin[c];
-#pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                const int g = __float_as_int(t ? m.b.w : m.a.w);
-                put4(q, k++, t ? m.c : m.a, t ? m.d : m.b, g < 0 ? g : (int)map[g]);
-            }
-        }
-    }
-    const float INF = __int_as_float(0x7f800000);
-    const float4 empty = make_float4(INF, INF, INF, 0.0f);
-    for (; k < 4; ++k) put4(q, k, empty, empty, 0);
-    out[map[i]] = q;
-}
-
-// Greedy surface-area collapse.  The children of the 4-wide node of binary
-// node b: start from b's two children and open the internal child whose box
-// has the largest surface area (lowest slot on ties) until there are four or
-// only leaves are left.  Returns the count; ids are binary node indices (>= 0)
-// or ~object.
+// The children of the wide node of binary node b, from b's two children:
+//   greedy (surface-area collapse): open the internal child whose box has
+//     the largest surface area (lowest slot on ties) until there are
+//     kBvhWidth or only leaves are left;
+//   level (the fallback for trees the greedy rule leaves too deep): open
+//     every internal child, log2(kBvhWidth) - 1 times, so the node holds the
+//     binary nodes 2 (width 4) or 3 (width 8) levels below b, or the leaves
+//     above them, and the wide tree is that many times shallower.
+// Returns the count; ids are binary node indices (>= 0) or ~object.
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
     return dx * dy + dy * dz + dz * dx;
 }
 
-__device__ __forceinline__ int greedy_children(const BvhNode* __restrict__ bin, int b, int id[4], float4 lo[4],
-                                               float4 hi[4]) {
+constexpr int W = kBvhWidth;
+
+__device__ __forceinline__ int wide_children(const BvhNode* __restrict__ bin, int b, bool level, int (&id)[W],
+                                             float4 (&lo)[W], float4 (&hi)[W]) {
     const BvhNode nd = bin[b];
     id[0] = __float_as_int(nd.a.w);
     lo[0] = nd.a;
@@ -390,7 +348,24 @@ __device__ __forceinline__ int greedy_children(const BvhNode* __restrict__ bin, 
     lo[1] = nd.c;
     hi[1] = nd.d;
     int k = 2;
-    while (k < 4) {
+    if (level) {
+        for (int round = 0; round < (W == 8 ? 2 : 1); ++round) {
+            const int kk = k;
+            for (int j = 0; j < kk; ++j) {
+                if (id[j] < 0) continue;
+                const BvhNode m = bin[id[j]];
+                id[j] = __float_as_int(m.a.w);
+                lo[j] = m.a;
+                hi[j] = m.b;
+                id[k] = __float_as_int(m.b.w);
+                lo[k] = m.c;
+                hi[k] = m.d;
+                ++k;
+            }
+        }
+        return k;
+    }
+    while (k < W) {
         int best = -1;
         float ba = -1.0f;
         for (int j = 0; j < k; ++j) {
@@ -416,43 +391,62 @@ __device__ __forceinline__ int greedy_children(const BvhNode* __restrict__ bin, 
 
 // Level pass 1: the number of internal children of each frontier node.
 __global__ void collapse_count_kernel(const BvhNode* __restrict__ bin, const int2* __restrict__ front, uint32_t m,
-                                      uint32_t* __restrict__ count) {
+                                      bool level, uint32_t* __restrict__ count) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
-    int id[4];
-    float4 lo[4], hi[4];
-    const int k = greedy_children(bin, front[i].x, id, lo, hi);
+    int id[W];
+    float4 lo[W], hi[W];
+    const int k = wide_children(bin, front[i].x, level, id, lo, hi);
     uint32_t c = 0;
     for (int j = 0; j < k; ++j) c += id[j] >= 0 ? 1u : 0u;
     count[i] = c;
 }
 
-// Level pass 2: write frontier node i's 4-wide node at front[i].y; its
-// internal children become nodes next_base + off[i] + r (r their rank in
-// slot order) and the next level's frontier entries off[i] + r.
+// Level pass 2: write frontier node i's wide node at front[i].y.  Its
+// internal children take the first slots (in the order wide_children gives
+// them) and become nodes next_base + off[i] + r, r = 0, 1, ..., and the next
+// level's frontier entries off[i] + r; the leaf children follow.
 __global__ void collapse_write_kernel(const BvhNode* __restrict__ bin, const int2* __restrict__ front, uint32_t m,
-                                      const uint32_t* __restrict__ off, uint32_t next_base, Bvh4Node* out,
-                                      int2* __restrict__ next) {
+                                      bool level, const uint32_t* __restrict__ off, uint32_t next_base,
+                                      BvhWideNode* out, int2* __restrict__ next) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
-    int id[4];
-    float4 lo[4], hi[4];
-    const int k = greedy_children(bin, front[i].x, id, lo, hi);
-    Bvh4Node q;
-    uint32_t r = off[i];
-    for (int j = 0; j < k; ++j) {
-        if (id[j] < 0) {
-            put4(q, j, lo[j], hi[j], id[j]);
-        } else {
-            const int idx = (int)(next_base + r);
-            put4(q, j, lo[j], hi[j], idx);
-            next[r] = make_int2(id[j], idx);
-            ++r;
+    int id[W];
+    float4 lo[W], hi[W];
+    const int k = wide_children(bin, front[i].x, level, id, lo, hi);
+    const float INF = __int_as_float(0x7f800000);
+    BvhWideNode q;
+    for (int j = 0; j < W; ++j) {
+        q.pl[0][j] = q.pl[2][j] = q.pl[4][j] = INF;
+        q.pl[1][j] = q.pl[3][j] = q.pl[5][j] = -INF;
+        q.child[j] = 0;
+    }
+    q.leaves = 0u;
+    q.first = (int)(next_base + off[i]);
+    for (uint32_t& w : q.pad) w = 0u;
+    uint32_t r = 0;
+    int slot = 0;
+    for (int pass = 0; pass < 2; ++pass) {  // internal children, then leaves
+        for (int j = 0; j < k; ++j) {
+            if ((id[j] >= 0) != (pass == 0)) continue;
+            q.pl[0][slot] = lo[j].x;
+            q.pl[1][slot] = hi[j].x;
+            q.pl[2][slot] = lo[j].y;
+            q.pl[3][slot] = hi[j].y;
+            q.pl[4][slot] = lo[j].z;
+            q.pl[5][slot] = hi[j].z;
+            if (id[j] < 0) {
+                q.child[slot] = id[j];
+                q.leaves |= 1u << slot;
+            } else {
+                const int idx = (int)(next_base + off[i] + r);
+                q.child[slot] = idx;
+                next[off[i] + r] = make_int2(id[j], idx);
+                ++r;
+            }
+            ++slot;
         }
     }
-    const float INF = __int_as_float(0x7f800000);
-    const float4 empty = make_float4(INF, INF, INF, 0.0f);
-    for (int j = k; j < 4; ++j) put4(q, j, empty, empty, 0);
     out[front[i].y] = q;
 }
 
@@ -538,7 +532,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     out.scene_r = upr(scene_r * 1.0001);
     out.o_max = down(o_max);
 
-    // Device buffers: the 4-wide nodes + prims are kept; the rest (binary
+    // Device buffers: the wide nodes + prims are kept; the rest (binary
     // nodes included) is build scratch.
     const size_t n_int = n >= 2 ? (size_t)n - 1 : 1;
     cudaError_t e = dev_malloc((void**)&out.prims, prims.size() * sizeof(float4));
@@ -549,7 +543,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     if (e == cudaSuccess)
         e = cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n_int, s);
     // scratch: box (2n float4) | binary nodes (n-1) | keys, keys2, vals, vals2 (4n u32) | parents (2n int) |
-    //          flags, even, map (3n u32) | two collapse frontiers (n-1 int2 each) | depth | sort tmp | scan tmp
+    //          flags, counts, map (3n u32) | two collapse frontiers (n-1 int2 each) | depth | sort tmp | scan tmp
     const size_t box_b = 2 * (size_t)n * sizeof(float4);
     const size_t bin_b = n_int * sizeof(BvhNode);
     const size_t u32_b = (size_t)n * 4;
@@ -578,7 +572,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     int* parent_node = (int*)take(u32_b);
     int* parent_leaf = (int*)take(u32_b);
     uint32_t* flags = (uint32_t*)take(u32_b);
-    uint32_t* even = (uint32_t*)take(u32_b);
+    uint32_t* counts = (uint32_t*)take(u32_b);
     uint32_t* map = (uint32_t*)take(u32_b);
     int2* front = (int2*)take(front_b);
     int2* front_next = (int2*)take(front_b);
@@ -612,7 +606,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
         // Karras tree, refit, then treelet restructuring passes (each pass
         // bottom-up; the leaves' starting parents are snapshot into keys, free
         // after the sort).  Restructuring can deepen the tree: should it pass
-        // the depth the 4-wide traversal allows, the tree is rebuilt without.
+        // the depth the wide traversal allows, the tree is rebuilt without.
         for (int passes = kRestructurePasses;; passes = 0) {
             karras_kernel<<<GI, B, 0, s>>>(keys2, vals2, (int)n, bin, parent_node, parent_leaf);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -637,61 +631,45 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
             if (depth <= 62 || passes == 0) break;
         }
 
-        // Greedy surface-area collapse, one level per pass (count, scan,
-        // write).  At most n - 1 4-wide nodes (each holds >= 2 children).
-        e = dev_malloc((void**)&out.nodes, n_int * sizeof(Bvh4Node));
+        // Collapse to wide nodes, one level per pass (count, scan, write): the
+        // greedy surface-area rule, or, should that tree be deeper than the
+        // traversal stack allows (kBvhMaxLevels, width - 1 entries each), the
+        // level rule (the binary tree is at most 63 deep: at most 32 levels at
+        // width 4, 21 at width 8).  At most n - 1 wide nodes (each holds >= 2
+        // children).
+        static_assert(kBvhMaxLevels >= (kBvhWidth == 8 ? 21 : 32), "stack too short for the level rule");
+        e = dev_malloc((void**)&out.nodes, n_int * sizeof(BvhWideNode));
         if (e != cudaSuccess) return e;
-        const int2 root = make_int2(0, 0);
-        e = cudaMemcpyAsync(front, &root, sizeof(int2), cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return e;
-        uint32_t m = 1, total = 1, levels = 0;
-        while (m > 0 && levels <= 32) {
-            ++levels;
-            const uint32_t GM = (m + B - 1) / B;
-            collapse_count_kernel<<<GM, B, 0, s>>>(bin, front, m, even);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
-            e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, even, map, (int)m, s);
+        uint32_t m = 1, total = 1;
+        for (int mode = 0; mode < 2; ++mode) {  // 0: greedy surface area, 1: level rule
+            const int2 root = make_int2(0, 0);
+            e = cudaMemcpyAsync(front, &root, sizeof(int2), cudaMemcpyHostToDevice, s);
             if (e != cudaSuccess) return e;
-            collapse_write_kernel<<<GM, B, 0, s>>>(bin, front, m, map, total, out.nodes, front_next);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
-            uint32_t tl[2] = {0, 0};
-            e = cudaMemcpyAsync(&tl[0], map + m - 1, 4, cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(&tl[1], even + m - 1, 4, cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) return e;
-            m = tl[0] + tl[1];
-            total += m;
-            std::swap(front, front_next);
+            m = 1;
+            total = 1;
+            uint32_t levels = 0;
+            while (m > 0 && levels < (uint32_t)kBvhMaxLevels) {
+                ++levels;
+                const uint32_t GM = (m + B - 1) / B;
+                collapse_count_kernel<<<GM, B, 0, s>>>(bin, front, m, mode != 0, counts);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, counts, map, (int)m, s);
+                if (e != cudaSuccess) return e;
+                collapse_write_kernel<<<GM, B, 0, s>>>(bin, front, m, mode != 0, map, total, out.nodes, front_next);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                uint32_t tl[2] = {0, 0};
+                e = cudaMemcpyAsync(&tl[0], map + m - 1, 4, cudaMemcpyDeviceToHost, s);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(&tl[1], counts + m - 1, 4, cudaMemcpyDeviceToHost, s);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) return e;
+                m = tl[0] + tl[1];
+                total += m;
+                std::swap(front, front_next);
+            }
+            if (m == 0) break;
         }
-        if (m == 0) {
-            out.nnodes = total;
-            e = cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) return e;
-            if (depth_out) *depth_out = depth;
-            cudaFree(out.scratch);
-            out.scratch = nullptr;
-            out.scratch_bytes = 0;
-            return cudaSuccess;
-        }
-        // Deeper than 32 levels (3 stack entries each): the even-depth collapse.
-        cudaFree(out.nodes);
-        out.nodes = nullptr;
-        even_depth_kernel<<<GI, B, 0, s>>>(parent_node, (int)n_int, even);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, even, map, (int)n_int, s);
-        if (e != cudaSuccess) return e;
-        uint32_t tail[2] = {0, 0};
-        e = cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[0], map + n_int - 1, 4, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&tail[1], even + n_int - 1, 4, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        out.nnodes = tail[0] + tail[1];
-        e = dev_malloc((void**)&out.nodes, (size_t)out.nnodes * sizeof(Bvh4Node));
-        if (e != cudaSuccess) return e;
-        collapse4_kernel<<<GI, B, 0, s>>>(bin, even, map, (int)n_int, out.nodes);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (m != 0) return cudaErrorUnknown;  // unreachable: the level rule's tree fits the stack
+        out.nnodes = total;
     }
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;

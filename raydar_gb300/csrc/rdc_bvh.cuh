@@ -2,11 +2,10 @@
 //
 // The reference tests every object (src/renderer/cpu.rs:344-352).  For large
 // scenes the kernels instead walk a linear BVH: Morton-ordered objects, a
-// Karras (2012) radix tree of N-1 internal nodes, collapsed into a 4-wide
-// tree (every binary node at even depth keeps its grandchildren, or its leaf
-// children, as up to four children): half the dependent node loads per ray,
-// four independent box tests per load.  The result must be the reference's
-// exactly:
+// Karras (2012) radix tree of N-1 internal nodes, collapsed into a wide tree
+// (each node takes up to kBvhWidth binary descendants as its children): a
+// fraction of the dependent node loads per ray, that many independent box
+// tests per load.  The result must be the reference's exactly:
 //   - leaves run the same exact sphere / cube tests as the brute-force loop;
 //   - the first-minimum rule (lowest object index among equal t) becomes a
 //     lexicographic minimum over (t, index), independent of visiting order;
@@ -42,12 +41,35 @@ struct alignas(16) BvhNode {
     float4 d;  // child 1 box max (xyz), 0
 };
 
-// 4-wide node, 128 bytes: child j's box in v[2j] (min xyz, child in w as
-// int bits: >= 0 node, < 0 leaf ~object) and v[2j+1] (max xyz).  An unused
-// slot has min = max = +inf, which no ray hits (1/d is never 0).
-struct alignas(16) Bvh4Node {
-    float4 v[8];
+#ifndef RDC_BVH_WIDTH
+#define RDC_BVH_WIDTH 4
+#endif
+constexpr int kBvhWidth = RDC_BVH_WIDTH;  // children per node: 4 or 8
+static_assert(kBvhWidth == 4 || kBvhWidth == 8, "node width");
+
+// Wide node (kBvhWidth children; 128 bytes at 4, 256 at 8), its children's
+// boxes stored plane by plane:
+//   pl[0][j] min.x of child j   pl[1][j] max.x
+//   pl[2][j] min.y              pl[3][j] max.y
+//   pl[4][j] min.z              pl[5][j] max.z
+// For a positive direction component a box's near plane on that axis is its
+// minimum, for a negative one its maximum, so a ray reads the near planes of
+// all children on an axis with one load and the far planes with another,
+// from offsets fixed per ray: the box test needs no per-child min/max to
+// order the planes.  child[j]: >= 0 node, < 0 ~object; the internal children
+// take the first slots, at consecutive node indices from `first` (slot j's
+// node is first + j).  leaves: bit j set when slot j holds an object.  An
+// unused slot has min = +inf, max = -inf: every ray's near plane there is
+// +inf and its far plane -inf, so it is never entered.
+struct alignas(32) BvhWideNode {
+    float pl[6][kBvhWidth];
+    int child[kBvhWidth];
+    uint32_t leaves;
+    int first;
+    uint32_t pad[kBvhWidth == 8 ? 6 : 2];
 };
+static_assert(sizeof(BvhWideNode) == 32 * kBvhWidth, "wide node layout");
+constexpr uint32_t kPlaneBytes = 4 * kBvhWidth;  // one plane of every child
 
 // BvhView (rdc_internal.hpp): nodes (root 0), prims (2 per object, scene
 // order: sphere (c, c.c) (r*r, 0, 0, kind); cube in the slab pair layout with
@@ -107,28 +129,66 @@ __device__ __forceinline__ void bvh_leaf(const BvhView& bv, const RayPre& r, int
     }
 }
 
-// Conservative slab test of a box [lo - m, hi + m] (m the per-ray growth):
-// with oa = (o + m) / d and ob = (o - m) / d per axis, the plane distances
-// are lo / d - oa and hi / d - ob, one FMA each.  Their rounding (a few ulp
-// of |o| + |lo| along the ray) is far inside the 2^-20 (|o| + 2R) part of m,
-// so the box's entry and exit are compared as computed.
-__device__ __forceinline__ bool bvh_box(float3 lo, float3 hi, float3 oa, float3 ob, float3 inv, float limit,
-                                        float& entry) {
-    const float lx = __fmaf_rn(lo.x, inv.x, -oa.x), hx = __fmaf_rn(hi.x, inv.x, -ob.x);
-    const float ly = __fmaf_rn(lo.y, inv.y, -oa.y), hy = __fmaf_rn(hi.y, inv.y, -ob.y);
-    const float lz = __fmaf_rn(lo.z, inv.z, -oa.z), hz = __fmaf_rn(hi.z, inv.z, -ob.z);
-    const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
-    const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
-    entry = tmin;
-    return fmaxf(tmin, 0.0f) <= fminf(tmax, limit);
+// Conservative slab tests of a node's children, boxes [lo - m, hi + m] (m
+// the per-ray growth).  Per axis, with oa = (o + m) / d and ob = (o - m) / d,
+// the plane distances are lo / d - oa and hi / d - ob, one FMA each; the near
+// one is lo's for d >= 0 (1/d carries d's sign, zeros included) and hi's
+// otherwise, which fixes per ray which plane each load returns and which
+// origin term goes with it.  Their rounding (a few ulp of |o| + |lo| along
+// the ray) is far inside the 2^-20 (|o| + 2R) part of m, so the box's entry
+// and exit are compared as computed; 2m also keeps far - near positive for
+// every non-empty box, so ordering the planes by the sign of 1/d gives the
+// same entry and exit as ordering them by value.
+struct BvhRayBox {
+    float inv[3];       // 1/d per axis
+    float nn[3], nf[3]; // -(near origin term), -(far origin term) per axis
+    uint32_t near_off;  // byte offsets of the near planes: x in bits 0-7, y 8-15, z 16-23
+};
+
+// One plane of every child (kBvhWidth floats) at byte offset off of node nb.
+__device__ __forceinline__ void ldg_planes(const char* nb, uint32_t off, float (&v)[kBvhWidth]) {
+    if constexpr (kBvhWidth == 8) {
+        float4 a, b;
+        ldg_pair(reinterpret_cast<const float4*>(nb + off), a, b);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(nb + off));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+}
+
+// Entry (max(0, near)) of every child box, and a bit per child whose box is
+// entered no later than limit and left no earlier than 0.
+__device__ __forceinline__ unsigned bvh_boxes(const char* nb, const BvhRayBox& R, float limit,
+                                              float (&e)[kBvhWidth]) {
+    const uint32_t ox = R.near_off & 0xffu, oy = (R.near_off >> 8) & 0xffu, oz = R.near_off >> 16;
+    float nx[kBvhWidth], fx[kBvhWidth], ny[kBvhWidth], fy[kBvhWidth], nz[kBvhWidth], fz[kBvhWidth];
+    ldg_planes(nb, ox, nx);
+    ldg_planes(nb, ox ^ kPlaneBytes, fx);
+    ldg_planes(nb, oy, ny);
+    ldg_planes(nb, oy ^ kPlaneBytes, fy);
+    ldg_planes(nb, oz, nz);
+    ldg_planes(nb, oz ^ kPlaneBytes, fz);
+    unsigned hits = 0u;
+#pragma unroll
+    for (int j = 0; j < kBvhWidth; ++j) {
+        const float n = fmax3(__fmaf_rn(nx[j], R.inv[0], R.nn[0]), __fmaf_rn(ny[j], R.inv[1], R.nn[1]),
+                              fmaxf(__fmaf_rn(nz[j], R.inv[2], R.nn[2]), 0.0f));
+        const float f = fmin3(__fmaf_rn(fx[j], R.inv[0], R.nf[0]), __fmaf_rn(fy[j], R.inv[1], R.nf[1]),
+                              fminf(__fmaf_rn(fz[j], R.inv[2], R.nf[2]), limit));
+        e[j] = n;
+        hits |= (n <= f ? 1u : 0u) << j;
+    }
+    return hits;
 }
 
 // One ray's traversal, resumable one node visit at a time.  The stack lives
-// with the caller: a binary Karras tree over 30-bit codes with 32-bit index
-// tie-breaks is at most 63 deep, the 4-wide tree at most 32, and a visit
-// leaves at most 3 siblings pending per level.
+// with the caller: a visit leaves at most kBvhWidth - 1 siblings pending, and
+// the build keeps the wide tree at most kBvhMaxLevels deep (a binary Karras
+// tree over 30-bit codes with 32-bit index tie-breaks is at most 63 deep).
 struct BvhTrav {
-    float3 oa, ob, inv;  // (o + m) / d, (o - m) / d per axis (m: see the file comment), 1/d
+    BvhRayBox box;       // the ray's per-axis box-test terms
     float best;          // closest hit so far (+inf: none)
     int bidx;            // its object (-1: none)
     int cur;             // next node to visit; -1 when no node is left
@@ -137,7 +197,8 @@ struct BvhTrav {
     unsigned lmask;      // the traversal is over when cur < 0 and lmask == 0
 };
 
-constexpr int kBvhStack = 96;
+constexpr int kBvhStack = kBvhWidth == 8 ? 160 : 96;
+constexpr int kBvhMaxLevels = kBvhStack / (kBvhWidth - 1);  // 22 at width 8, 32 at width 4
 
 __device__ __forceinline__ void bvh_leaf_any(const BvhView& bv, const RayPre& r, bool fast, int obj, float& best,
                                              int& bidx) {
@@ -171,10 +232,21 @@ __device__ __forceinline__ void bvh_begin(const BvhView& bv, const RayPre& r, bo
     // as if it were 1/cap): cap * (|o| + 2R + 1) stays below 1e37, so no
     // plane distance overflows.
     const float cap = fminf(1e30f, 1e37f / (olen + 2.0f * bv.scene_r + 1.0f));
-    auto inv1 = [cap](float v) { return fabsf(v) * cap < 1.0f ? copysignf(cap, v) : 1.0f / v; };
-    T.inv = make_float3(inv1(r.d.x), inv1(r.d.y), inv1(r.d.z));
-    T.oa = make_float3((r.o.x + m) * T.inv.x, (r.o.y + m) * T.inv.y, (r.o.z + m) * T.inv.z);
-    T.ob = make_float3((r.o.x - m) * T.inv.x, (r.o.y - m) * T.inv.y, (r.o.z - m) * T.inv.z);
+    // (r.rd is RN(1/d), the IEEE quotient 1.0f / d)
+    auto inv1 = [cap](float v, float rv) { return fabsf(v) * cap < 1.0f ? copysignf(cap, v) : rv; };
+    const float iv[3] = {inv1(r.d.x, r.rd.x), inv1(r.d.y, r.rd.y), inv1(r.d.z, r.rd.z)};
+    const float ov[3] = {r.o.x, r.o.y, r.o.z};
+    uint32_t off = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float oa = (ov[a] + m) * iv[a], ob = (ov[a] - m) * iv[a];
+        const bool neg = __float_as_uint(iv[a]) >> 31;  // near plane: the maximum (pl[2a + 1])
+        T.box.inv[a] = iv[a];
+        T.box.nn[a] = neg ? -ob : -oa;
+        T.box.nf[a] = neg ? -oa : -ob;
+        off |= (2u * kPlaneBytes * a + (neg ? kPlaneBytes : 0u)) << (8 * a);
+    }
+    T.box.near_off = off;
     T.cur = 0;
 }
 
@@ -188,6 +260,7 @@ constexpr int kShortStack = 16;
 
 struct LocalStack {
     uint2* a;
+    __device__ __forceinline__ void put(int i, uint2 e) { a[i] = e; }
     __device__ __forceinline__ void push(int& sp, uint2 e) { a[sp++] = e; }
     __device__ __forceinline__ uint2 pop(int& sp) { return a[--sp]; }
 };
@@ -196,6 +269,12 @@ struct SplitStack {
     uint2* sh;
     uint32_t stride;
     uint2* loc;
+    __device__ __forceinline__ void put(int i, uint2 e) {
+        if (i < kShortStack)
+            sh[(uint32_t)i * stride] = e;
+        else
+            loc[i - kShortStack] = e;
+    }
     __device__ __forceinline__ void push(int& sp, uint2 e) {
         if (sp < kShortStack)
             sh[(uint32_t)sp * stride] = e;
@@ -209,69 +288,82 @@ struct SplitStack {
     }
 };
 
-// Compare-exchange of (entry, node) pairs, ascending by entry.
-__device__ __forceinline__ void bvh_cswap(float& ka, int& va, float& kb, int& vb) {
-    const bool sw = kb < ka;
-    const float k = sw ? kb : ka;
-    const int v = sw ? vb : va;
-    kb = sw ? ka : kb;
-    vb = sw ? va : vb;
-    ka = k;
-    va = v;
+// Compare-exchange of two sort keys, ascending.
+__device__ __forceinline__ void bvh_cswap(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = umin(a, b);
+    b = umax(a, b);
+    a = lo;
 }
 
-// One node visit (T.cur >= 0, T.lmask == 0): the four child boxes; leaf
-// children hit are left in T.lmask for bvh_leaf_step (a warp tests them
-// together instead of one lane at a time inside the visit); the nearest
-// internal child hit is visited next and the others pushed, farthest first;
-// with none, the next stacked box still in front of the best hit, or none
-// (T.cur = -1).
+// Sort network on the visit's keys, ascending: 5 compare-exchanges for 4,
+// 19 for 8 (both halves, then Batcher's odd-even merge).
+__device__ __forceinline__ void bvh_sort4(uint32_t* k) {
+    bvh_cswap(k[0], k[1]);
+    bvh_cswap(k[2], k[3]);
+    bvh_cswap(k[0], k[2]);
+    bvh_cswap(k[1], k[3]);
+    bvh_cswap(k[1], k[2]);
+}
+__device__ __forceinline__ void bvh_sort(uint32_t (&k)[kBvhWidth]) {
+    bvh_sort4(k);
+    if constexpr (kBvhWidth == 8) {
+        bvh_sort4(k + 4);
+        bvh_cswap(k[0], k[4]);
+        bvh_cswap(k[1], k[5]);
+        bvh_cswap(k[2], k[6]);
+        bvh_cswap(k[3], k[7]);
+        bvh_cswap(k[2], k[4]);
+        bvh_cswap(k[3], k[5]);
+        bvh_cswap(k[1], k[2]);
+        bvh_cswap(k[3], k[4]);
+        bvh_cswap(k[5], k[6]);
+    }
+}
+
+// One node visit (T.cur >= 0, T.lmask == 0): the child boxes; leaf children
+// hit are left in T.lmask for bvh_leaf_step (a warp tests them together
+// instead of one lane at a time inside the visit); the nearest internal child
+// hit is visited next and the others pushed, farthest first; with none, the
+// next stacked box still in front of the best hit, or none (T.cur = -1).
+// Internal children are ordered by a key per slot: the entry distance's bits
+// (non-negative: ordered as unsigned integers) with the low bits replaced by
+// the slot, at most 7 ulp off the entry; the stack keeps the entry rounded
+// down to a multiple of 8 ulp, so its test against the best hit stays
+// conservative.
 template <class Stack>
 __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T, Stack& stack,
                                          BvhCounters& cnt) {
-    const float4* np = bv.nodes[checked_index(bv.oob, T.cur, bv.nnodes)].v;
-    float4 lo[4], hi[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) ldg_pair(np + 2 * j, lo[j], hi[j]);
+    const BvhWideNode* node = bv.nodes + checked_index(bv.oob, T.cur, bv.nnodes);
+    const char* nb = reinterpret_cast<const char*>(node);
+    const uint2 meta = __ldg(reinterpret_cast<const uint2*>(&node->leaves));  // (leaves, first)
     ++cnt.visits;
     // limit: skip a box whose entry exceeds best (relative slack for the box test's rounding)
     const float limit = T.best * 1.0000038f + 1e-30f;
-    float e[4];
-    int c[4];
-    unsigned hits = 0u;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        c[j] = __float_as_int(lo[j].w);
-        if (bvh_box(make_float3(lo[j].x, lo[j].y, lo[j].z), make_float3(hi[j].x, hi[j].y, hi[j].z), T.oa, T.ob,
-                    T.inv, limit, e[j]))
-            hits |= 1u << j;
-    }
-    T.lmask = hits & ((c[0] < 0 ? 1u : 0u) | (c[1] < 0 ? 2u : 0u) | (c[2] < 0 ? 4u : 0u) | (c[3] < 0 ? 8u : 0u));
+    float e[kBvhWidth];
+    const unsigned hits = bvh_boxes(nb, T.box, limit, e);
+    T.lmask = hits & meta.x;
     T.lnode = T.cur;
-    const float lim = limit;
-    const float INF = __int_as_float(0x7f800000);
-    float k0 = ((hits & 1u) && c[0] >= 0) ? e[0] : INF;
-    float k1 = ((hits & 2u) && c[1] >= 0) ? e[1] : INF;
-    float k2 = ((hits & 4u) && c[2] >= 0) ? e[2] : INF;
-    float k3 = ((hits & 8u) && c[3] >= 0) ? e[3] : INF;
-    int v0 = c[0], v1 = c[1], v2 = c[2], v3 = c[3];
-    bvh_cswap(k0, v0, k1, v1);
-    bvh_cswap(k2, v2, k3, v3);
-    bvh_cswap(k0, v0, k2, v2);
-    bvh_cswap(k1, v1, k3, v3);
-    bvh_cswap(k1, v1, k2, v2);
-    if (k0 != INF) {
-        // an entry is (node, entry distance bits): one 8-byte local store or load
-        if (k3 != INF) stack.push(T.sp, make_uint2((unsigned)v3, __float_as_uint(k3)));
-        if (k2 != INF) stack.push(T.sp, make_uint2((unsigned)v2, __float_as_uint(k2)));
-        if (k1 != INF) stack.push(T.sp, make_uint2((unsigned)v1, __float_as_uint(k1)));
-        T.cur = v0;
+    const unsigned inner = hits & ~meta.x;
+    const uint32_t NONE = 0xffffffffu;
+    const uint32_t SLOT = kBvhWidth - 1u;
+    uint32_t k[kBvhWidth];
+#pragma unroll
+    for (int j = 0; j < kBvhWidth; ++j)
+        k[j] = ((inner >> j) & 1u) ? (__float_as_uint(e[j]) & (0x7fffffffu & ~SLOT)) | (uint32_t)j : NONE;
+    bvh_sort(k);
+    const int first = (int)meta.y;
+    if (k[0] != NONE) {
+        // an entry is (node, entry distance bits): one 8-byte store or load
+#pragma unroll
+        for (int j = kBvhWidth - 1; j >= 1; --j)
+            if (k[j] != NONE) stack.push(T.sp, make_uint2((unsigned)(first + (int)(k[j] & SLOT)), k[j] & ~SLOT));
+        T.cur = first + (int)(k[0] & SLOT);
     } else {
         // pop the next box still in front of the best hit
         int next = -1;
         while (T.sp > 0) {
             const uint2 top = stack.pop(T.sp);
-            if (__uint_as_float(top.y) <= lim) {
+            if (__uint_as_float(top.y) <= limit) {
                 next = (int)top.x;
                 break;
             }
@@ -285,7 +377,7 @@ __device__ __forceinline__ void bvh_leaf_step(const BvhView& bv, const RayPre& r
                                               BvhCounters& cnt) {
     const int j = __ffs(T.lmask) - 1;
     T.lmask &= T.lmask - 1u;
-    const int child = __float_as_int(__ldg(&bv.nodes[checked_index(bv.oob, T.lnode, bv.nnodes)].v[2 * j].w));
+    const int child = __ldg(&bv.nodes[checked_index(bv.oob, T.lnode, bv.nnodes)].child[j]);
     ++cnt.tests;
     bvh_leaf_any(bv, r, fast, ~child, T.best, T.bidx);
 }
