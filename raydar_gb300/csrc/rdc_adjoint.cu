@@ -213,8 +213,8 @@ __device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7], uns
     const unsigned above = lane == 31 ? 0u : (peers & (0xffffffffu << (lane + 1)));
     int next = above ? __ffs(above) - 1 : lane;
     bool has = above != 0u;
-#pragma unroll
-    for (int round = 0; round < 5; ++round) {
+#pragma unroll 1
+    for (int round = 0; round < 5; ++round) {  // rolled: less code for the fetch-bound kernel
         float o[7];
 #pragma unroll
         for (int j = 0; j < 7; ++j) o[j] = __shfl_sync(FULL, c[j], next);
@@ -235,19 +235,31 @@ __device__ __forceinline__ void warp_add_grad(float* g, int obj, float c[7], uns
     }
 }
 
-// Resident blocks per SM the register budget is sized for (64 registers at 4;
-// 3, 4 and 5 measured within 2% of each other on config 4, 4 the fastest).
+// Resident blocks per SM the register budget is sized for: with the vertex
+// records in local memory 4 (64 registers; 3, 4 and 5 measured within 2% of
+// each other on config 4, 4 the fastest); with them in shared memory, which
+// holds 3 blocks of 6-bounce records, 3 (80 registers, fewer spills).
 #ifndef RDC_ADJ_MIN_BLOCKS
 #define RDC_ADJ_MIN_BLOCKS 4
 #endif
+#ifndef RDC_ADJ_SH_MIN_BLOCKS
+#define RDC_ADJ_SH_MIN_BLOCKS 3
+#endif
 
-template <bool kBvh>
-__global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kernel(const AdjParams P) {
+// kShRec: the vertex records in the block's shared memory, after the
+// gradient table: thread t's at word t * shared_vert_stride (an odd number
+// of words, so a warp reading one field of one vertex hits 32 banks), which
+// keeps them out of the L1 and L2 the replay's loads use; otherwise a
+// per-thread local array.
+template <bool kBvh, bool kShRec>
+__global__ void __launch_bounds__(kRenderBlock, kShRec ? RDC_ADJ_SH_MIN_BLOCKS : RDC_ADJ_MIN_BLOCKS)
+    adjoint_kernel(const AdjParams P) {
     extern __shared__ float4 smem[];
     const unsigned FULL = 0xffffffffu;
     float4* s_rec = smem;
     int4* s_runs = reinterpret_cast<int4*>(smem + (kBvh ? 0u : P.sc.nrec));
     float* s_grad = reinterpret_cast<float*>(s_runs + (kBvh ? 0u : P.sc.nruns));
+    float* s_vert = s_grad + (P.smem_grad ? 8u * P.sc.nobj : 0u);
     __shared__ __align__(8) uint64_t s_bar;
     if (P.smem_grad)
         for (uint32_t i = threadIdx.x; i < 8u * P.sc.nobj; i += blockDim.x) s_grad[i] = 0.0f;
@@ -266,9 +278,14 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
     const uint64_t rounds = (P.npaths + stride - 1) / stride;  // the same for every thread
     for (uint64_t it = 0; it < rounds; ++it) {
         const uint64_t path = it * stride + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-        AdjVert v[kAdjMaxBounces];
+        AdjVert v_local[kShRec ? 1 : kAdjMaxBounces];
+        AdjVert* const v =
+            kShRec ? reinterpret_cast<AdjVert*>(s_vert + threadIdx.x * P.shared_vert_stride) : v_local;
         int nv = 0;
         V3 gw = mk(0.f, 0.f, 0.f);
+        V3 d = mk(0.f, 0.f, 0.f), atten = mk(1.f, 1.f, 1.f);
+        bool active = false, missed = false;
+        bool emit_after_first = false;  // an emissive hit after vertex 0
         if (path < P.npaths) {
             const uint32_t pix = (uint32_t)(path / P.nspp);
             const uint32_t sample = P.s0 + (uint32_t)(path % P.nspp);
@@ -277,11 +294,9 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
             gw = mk(P.dl[px3] * inv_n, P.dl[px3 + 1] * inv_n, P.dl[px3 + 2] * inv_n);
             if (gw.x != 0.0f || gw.y != 0.0f || gw.z != 0.0f) {
                 // replay (the forward kernels' arithmetic, bit for bit)
-                V3 o, d;
+                active = true;
+                V3 o;
                 primary_ray(P.sc, pix % P.sc.width, pix / P.sc.width, o, d);
-                V3 atten = mk(1.f, 1.f, 1.f);
-                bool missed = false;
-                bool emit_after_first = false;  // an emissive hit after vertex 0
                 for (uint32_t b = 0; b < P.max_bounces; ++b) {
                     ++segs;
                     const RayPre r = ray_pre(o, d, P.sc.neg_zero);
@@ -320,48 +335,56 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
                     o = no;
                     d = nd;
                 }
-                // A path that ends without a miss gathers only emission: with no
-                // emissive hit after its first vertex every coin weight is zero
-                // and nothing depends on a direction, so its sweep adds nothing.
-                const bool sweep = missed || emit_after_first;
-                // reverse sweep: S = the radiance gathered after the current
-                // vertex's scatter, suf = the albedos after it
-                V3 go = mk(0.f, 0.f, 0.f), gd = mk(0.f, 0.f, 0.f);
-                V3 sky = mk(0.f, 0.f, 0.f), S = mk(0.f, 0.f, 0.f);
-                if (missed) {
-                    sky = world_sample(P.sc, d);
-                    S = mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z);
-                    if (P.sc.world_kind == 0u) {
-                        // sky = bottom + (top - bottom) (d.y / |d| + 1) / 2
-                        const float coef = 0.5f * (gw.x * atten.x * (P.sc.top[0] - P.sc.bottom[0]) +
-                                                   gw.y * atten.y * (P.sc.top[1] - P.sc.bottom[1]) +
-                                                   gw.z * atten.z * (P.sc.top[2] - P.sc.bottom[2]));
-                        const float len = sqrtf(vdot(d, d));
-                        const float cosv = d.y / len;
-                        gd = vmul(vsub(mk(0.f, 1.f, 0.f), vmul(d, cosv / len)), coef / len);
-                    }
-                }
-                V3 suf = mk(1.f, 1.f, 1.f);
-                if (!sweep) {
-                    for (int k = 0; k < nv; ++k) {
-                        v[k].o = mk(0.f, 0.f, 0.f);
-                        v[k].t = 0.0f;
-                    }
-                }
-                for (int k = sweep ? nv - 1 : -1; k >= 0; --k) {
-                    AdjVert& vk = v[k];
-                    const int obj = (int)(vk.objf & 0xFFFFFFu);
-                    const MatDev m = load_mat(P.sc.mat, (int)checked_index(P.sc.oob, obj, P.sc.nobj));
-                    const V3 s = vk.s;
-                    const float wk = gw.x * S.x + gw.y * S.y + gw.z * S.z;
-                    const float gr = vertex_vjp(P.sc, vk, m, s, wk, go, gd);
-                    vk.o = mk(gw.x * sky.x * suf.x, gw.y * sky.y * suf.y, gw.z * sky.z * suf.z);
-                    vk.t = gr;
-                    suf = mk(suf.x * m.a.x, suf.y * m.a.y, suf.z * m.a.z);
-                    S = mk(S.x + m.b.x, S.y + m.b.y, S.z + m.b.z);
-                }
             }
         }
+        // The block's warps go from replay to sweep to accumulation together:
+        // the three phases' code does not fit the instruction cache at once,
+        // and warps spread over all three stalled on instruction fetch
+        // (config 4 backward 10.2 -> 8.3 ms with the barriers).
+        __syncthreads();
+        if (active) {
+            // A path that ends without a miss gathers only emission: with no
+            // emissive hit after its first vertex every coin weight is zero
+            // and nothing depends on a direction, so its sweep adds nothing.
+            const bool sweep = missed || emit_after_first;
+            // reverse sweep: S = the radiance gathered after the current
+            // vertex's scatter, suf = the albedos after it
+            V3 go = mk(0.f, 0.f, 0.f), gd = mk(0.f, 0.f, 0.f);
+            V3 sky = mk(0.f, 0.f, 0.f), S = mk(0.f, 0.f, 0.f);
+            if (missed) {
+                sky = world_sample(P.sc, d);
+                S = mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z);
+                if (P.sc.world_kind == 0u) {
+                    // sky = bottom + (top - bottom) (d.y / |d| + 1) / 2
+                    const float coef = 0.5f * (gw.x * atten.x * (P.sc.top[0] - P.sc.bottom[0]) +
+                                               gw.y * atten.y * (P.sc.top[1] - P.sc.bottom[1]) +
+                                               gw.z * atten.z * (P.sc.top[2] - P.sc.bottom[2]));
+                    const float len = sqrtf(vdot(d, d));
+                    const float cosv = d.y / len;
+                    gd = vmul(vsub(mk(0.f, 1.f, 0.f), vmul(d, cosv / len)), coef / len);
+                }
+            }
+            V3 suf = mk(1.f, 1.f, 1.f);
+            if (!sweep) {
+                for (int k = 0; k < nv; ++k) {
+                    v[k].o = mk(0.f, 0.f, 0.f);
+                    v[k].t = 0.0f;
+                }
+            }
+            for (int k = sweep ? nv - 1 : -1; k >= 0; --k) {
+                AdjVert& vk = v[k];
+                const int obj = (int)(vk.objf & 0xFFFFFFu);
+                const MatDev m = load_mat(P.sc.mat, (int)checked_index(P.sc.oob, obj, P.sc.nobj));
+                const V3 s = vk.s;
+                const float wk = gw.x * S.x + gw.y * S.y + gw.z * S.z;
+                const float gr = vertex_vjp(P.sc, vk, m, s, wk, go, gd);
+                vk.o = mk(gw.x * sky.x * suf.x, gw.y * sky.y * suf.y, gw.z * sky.z * suf.z);
+                vk.t = gr;
+                suf = mk(suf.x * m.a.x, suf.y * m.a.y, suf.z * m.a.z);
+                S = mk(S.x + m.b.x, S.y + m.b.y, S.z + m.b.z);
+            }
+        }
+        __syncthreads();
         // warp-converged accumulation over vertex slots; pre = the albedos
         // before vertex k, which completes its albedo gradient
         const int maxnv = (int)__reduce_max_sync(FULL, (unsigned)nv);
@@ -398,25 +421,44 @@ __global__ void __launch_bounds__(kRenderBlock, RDC_ADJ_MIN_BLOCKS) adjoint_kern
 
 }  // namespace
 
-size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad) {
+uint32_t adjoint_shared_vert_stride(uint32_t bounces) {
+    const uint32_t w = bounces * (uint32_t)(sizeof(AdjVert) / 4);
+    return w | 1u;
+}
+
+size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad, uint32_t shared_vert_bounces, int block) {
     size_t b = bvh ? 0 : 16u * ((size_t)sc.nrec + sc.nruns);
     if (smem_grad) b += 32u * (size_t)sc.nobj;
+    if (shared_vert_bounces) b += 4u * (size_t)adjoint_shared_vert_stride(shared_vert_bounces) * (size_t)block;
     return b;
 }
 
-cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm) {
-    const void* fn = bvh ? (const void*)adjoint_kernel<true> : (const void*)adjoint_kernel<false>;
+static const void* adjoint_fn(bool bvh, bool sh) {
+    if (bvh) return sh ? (const void*)adjoint_kernel<true, true> : (const void*)adjoint_kernel<true, false>;
+    return sh ? (const void*)adjoint_kernel<false, true> : (const void*)adjoint_kernel<false, false>;
+}
+
+cudaError_t adjoint_occupancy(bool bvh, bool shared_vert, int block, size_t smem, int* blocks_per_sm) {
+    const void* fn = adjoint_fn(bvh, shared_vert);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
 }
 
-cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, size_t smem, cudaStream_t s) {
-    if (bvh)
-        adjoint_kernel<true><<<grid, block, smem, s>>>(p);
-    else
-        adjoint_kernel<false><<<grid, block, smem, s>>>(p);
+cudaError_t launch_adjoint(const AdjParams& p, bool bvh, bool shared_vert, int grid, int block, size_t smem,
+                           cudaStream_t s) {
+    if (bvh) {
+        if (shared_vert)
+            adjoint_kernel<true, true><<<grid, block, smem, s>>>(p);
+        else
+            adjoint_kernel<true, false><<<grid, block, smem, s>>>(p);
+    } else {
+        if (shared_vert)
+            adjoint_kernel<false, true><<<grid, block, smem, s>>>(p);
+        else
+            adjoint_kernel<false, false><<<grid, block, smem, s>>>(p);
+    }
     return cudaGetLastError();
 }
 

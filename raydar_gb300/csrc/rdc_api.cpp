@@ -22,6 +22,14 @@ using rdc::MatDev;
 
 // Shared memory a block may use for the staged scene (records + runs).
 constexpr size_t kMaxSceneSmem = 200 * 1024;
+// Dynamic shared memory a block may use at all (227 KB on sm_103a).
+constexpr size_t kMaxDynSmem = 227 * 1024;
+#ifndef RDC_ADJ_SHARED_VERT_MIN_BLOCKS
+#define RDC_ADJ_SHARED_VERT_MIN_BLOCKS 3
+#endif
+// The adjoint keeps its vertex records in shared memory only while this many
+// 256-thread blocks still fit on an SM.
+constexpr int kAdjSharedVertMinBlocks = RDC_ADJ_SHARED_VERT_MIN_BLOCKS;
 constexpr size_t kCounters = 8;       // device counters per context
 constexpr size_t kErrorCounter = 4;   // index of the device-error count
 constexpr size_t kBoundsCounter = 5;  // out-of-range indices caught (bounds-checked build)
@@ -753,23 +761,40 @@ rdc_status rdc_backward(rdc_ctx* ctx, const float* dl_dimage, float* grad_albedo
         p.key0 = (uint32_t)ctx->adj_seed;
         p.key1 = (uint32_t)(ctx->adj_seed >> 32);
         p.npaths = (uint64_t)npix * ctx->adj_n;
+        p.shared_vert_stride = 0;
         p.segments = ctx->d_counters + 1;
         p.errors = ctx->d_counters + kErrorCounter;
         const bool bvh = ctx->bvh_active;
         if (!bvh && !ctx->brute_fits)
             return fail(ctx, RDC_ERR_LIMIT, "rdc_backward: brute force needs the records in shared memory");
-        size_t smem = rdc::adjoint_smem_bytes(ctx->view, bvh, true);
-        p.smem_grad = smem <= kMaxSceneSmem ? 1u : 0u;
-        if (!p.smem_grad) smem = rdc::adjoint_smem_bytes(ctx->view, bvh, false);
         const int block = rdc::kRenderBlock;
+        size_t smem = rdc::adjoint_smem_bytes(ctx->view, bvh, true, 0, block);
+        p.smem_grad = smem <= kMaxSceneSmem ? 1u : 0u;
+        if (!p.smem_grad) smem = rdc::adjoint_smem_bytes(ctx->view, bvh, false, 0, block);
         int per_sm = 0;
-        RDC_CUDA(ctx, rdc::adjoint_occupancy(bvh, block, smem, &per_sm));
+        RDC_CUDA(ctx, rdc::adjoint_occupancy(bvh, false, block, smem, &per_sm));
         if (per_sm < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_backward: scene does not fit in shared memory");
+        // Vertex records in shared memory when that still leaves
+        // kAdjSharedVertMinBlocks blocks per SM (short paths: 6 bounces at 256
+        // threads is 66 KB per block), else in local memory.
+        bool shared_vert = false;
+        {
+            const size_t smem_sh = rdc::adjoint_smem_bytes(ctx->view, bvh, p.smem_grad != 0u, p.max_bounces, block);
+            int per_sm_sh = 0;
+            if (smem_sh <= kMaxDynSmem && rdc::adjoint_occupancy(bvh, true, block, smem_sh, &per_sm_sh) == cudaSuccess &&
+                per_sm_sh >= kAdjSharedVertMinBlocks) {
+                shared_vert = true;
+                smem = smem_sh;
+                per_sm = per_sm_sh;
+                p.shared_vert_stride = rdc::adjoint_shared_vert_stride(p.max_bounces);
+            }
+            (void)cudaGetLastError();
+        }
         uint64_t grid = (uint64_t)ctx->num_sms * per_sm;
         const uint64_t need = (p.npaths + block - 1) / block;
         if (grid > need) grid = need;
         RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-        RDC_CUDA(ctx, rdc::launch_adjoint(p, bvh, (int)grid, block, smem, ctx->stream));
+        RDC_CUDA(ctx, rdc::launch_adjoint(p, bvh, shared_vert, (int)grid, block, smem, ctx->stream));
         RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
         ctx->last_timed = true;
         ctx->last_launches = 1;

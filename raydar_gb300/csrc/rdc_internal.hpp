@@ -115,11 +115,18 @@ struct AdjParams {
     uint64_t npaths;    // npix * nspp
     unsigned long long* segments;
     uint32_t smem_grad; // 1: per-block shared accumulators (8 * nobj floats)
+    uint32_t shared_vert_stride;  // words between threads' vertex records in shared memory (shared records only)
     unsigned long long* errors;  // device errors (shared-memory staging that did not complete)
 };
-size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad);
-cudaError_t adjoint_occupancy(bool bvh, int block, size_t smem, int* blocks_per_sm);
-cudaError_t launch_adjoint(const AdjParams& p, bool bvh, int grid, int block, size_t smem, cudaStream_t s);
+// Dynamic shared memory of the adjoint kernel: staged records (brute force),
+// the gradient table (smem_grad) and, for shared_vert_bounces > 0, that many
+// vertex records per thread of a block of `block` threads, each thread's
+// adjoint_shared_vert_stride(bounces) words apart.
+uint32_t adjoint_shared_vert_stride(uint32_t bounces);
+size_t adjoint_smem_bytes(const SceneView& sc, bool bvh, bool smem_grad, uint32_t shared_vert_bounces, int block);
+cudaError_t adjoint_occupancy(bool bvh, bool shared_vert, int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_adjoint(const AdjParams& p, bool bvh, bool shared_vert, int grid, int block, size_t smem,
+                           cudaStream_t s);
 
 // The message rdc_last_error(NULL) returns on this thread (calls without a
 // context: rdc_create, the .rscn reader/writer).
