@@ -252,7 +252,7 @@ rdc_status apply_accel(rdc_ctx* ctx, bool scene_changed) {
     if (depth > 64) {
         ctx->bvh.release();
         ctx->bvh_active = false;
-        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the traversal stack allows (width - 1 entries per wide level)");
+        return fail(ctx, RDC_ERR_LIMIT, "LBVH deeper than the traversal stack allows (3 entries per 4-wide level)");
     }
     ctx->bvh_active = n > 0;
     ctx->bvh_depth = depth;

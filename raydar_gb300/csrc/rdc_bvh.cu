@@ -16,15 +16,15 @@
 //   6b. tree depth (Karras trees over 30-bit codes with position tie-breaks
 //      are at most 63 deep; a restructured tree deeper than 62 is rebuilt
 //      without restructuring)
-//   7. collapse to wide nodes (kBvhWidth children), top down one level per
-//      pass: a wide node starts from its binary node's two children and opens
-//      the internal child of largest surface area until it is full (a greedy
-//      surface-area collapse); nodes are numbered level by level through a prefix sum
+//   7. collapse to 4-wide nodes, top down one level per pass: a 4-wide node
+//      starts from its binary node's two children and opens the internal
+//      child of largest surface area until it has four (a greedy surface-area
+//      collapse); nodes are numbered level by level through a prefix sum
 //      (CUB), so the layout is deterministic and every node's internal
 //      children have consecutive indices.  If that tree would be deeper than
-//      the traversal stack allows, every internal child is opened a fixed
-//      number of times instead (each node takes the binary nodes 2 or 3
-//      levels below its own), which divides the depth by that many.
+//      the traversal stack allows, every internal child is opened once
+//      instead (each node takes its binary node's grandchildren), which
+//      halves the depth.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -322,14 +322,13 @@ __global__ void restructure_kernel(const int* __restrict__ parent_leaf_start, in
     }
 }
 
-// The children of the wide node of binary node b, from b's two children:
+// The children of the 4-wide node of binary node b, from b's two children:
 //   greedy (surface-area collapse): open the internal child whose box has
-//     the largest surface area (lowest slot on ties) until there are
-//     kBvhWidth or only leaves are left;
+//     the largest surface area (lowest slot on ties) until there are four or
+//     only leaves are left;
 //   level (the fallback for trees the greedy rule leaves too deep): open
-//     every internal child, log2(kBvhWidth) - 1 times, so the node holds the
-//     binary nodes 2 (width 4) or 3 (width 8) levels below b, or the leaves
-//     above them, and the wide tree is that many times shallower.
+//     every internal child once, so the node holds b's grandchildren and its
+//     leaf children, and the 4-wide tree is half as deep as the binary one.
 // Returns the count; ids are binary node indices (>= 0) or ~object.
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
@@ -349,19 +348,17 @@ __device__ __forceinline__ int wide_children(const BvhNode* __restrict__ bin, in
     hi[1] = nd.d;
     int k = 2;
     if (level) {
-        for (int round = 0; round < (W == 8 ? 2 : 1); ++round) {
-            const int kk = k;
-            for (int j = 0; j < kk; ++j) {
-                if (id[j] < 0) continue;
-                const BvhNode m = bin[id[j]];
-                id[j] = __float_as_int(m.a.w);
-                lo[j] = m.a;
-                hi[j] = m.b;
-                id[k] = __float_as_int(m.b.w);
-                lo[k] = m.c;
-                hi[k] = m.d;
-                ++k;
-            }
+        const int kk = k;
+        for (int j = 0; j < kk; ++j) {
+            if (id[j] < 0) continue;
+            const BvhNode m = bin[id[j]];
+            id[j] = __float_as_int(m.a.w);
+            lo[j] = m.a;
+            hi[j] = m.b;
+            id[k] = __float_as_int(m.b.w);
+            lo[k] = m.c;
+            hi[k] = m.d;
+            ++k;
         }
         return k;
     }
@@ -402,23 +399,25 @@ __global__ void collapse_count_kernel(const BvhNode* __restrict__ bin, const int
     count[i] = c;
 }
 
-// Level pass 2: write frontier node i's wide node at front[i].y.  Its
+// Level pass 2: write frontier node i's 4-wide node at front[i].y.  Its
 // internal children take the first slots (in the order wide_children gives
 // them) and become nodes next_base + off[i] + r, r = 0, 1, ..., and the next
 // level's frontier entries off[i] + r; the leaf children follow.
 __global__ void collapse_write_kernel(const BvhNode* __restrict__ bin, const int2* __restrict__ front, uint32_t m,
                                       bool level, const uint32_t* __restrict__ off, uint32_t next_base,
-                                      BvhWideNode* out, int2* __restrict__ next) {
+                                      Bvh4Node* out, int2* __restrict__ next) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     int id[W];
     float4 lo[W], hi[W];
     const int k = wide_children(bin, front[i].x, level, id, lo, hi);
     const float INF = __int_as_float(0x7f800000);
-    BvhWideNode q;
+    Bvh4Node q;
     for (int j = 0; j < W; ++j) {
-        q.pl[0][j] = q.pl[2][j] = q.pl[4][j] = INF;
-        q.pl[1][j] = q.pl[3][j] = q.pl[5][j] = -INF;
+        for (int a = 0; a < 3; ++a) {
+            q.pl[4 * a][j] = q.pl[4 * a + 3][j] = INF;
+            q.pl[4 * a + 1][j] = q.pl[4 * a + 2][j] = -INF;
+        }
         q.child[j] = 0;
     }
     q.leaves = 0u;
@@ -429,12 +428,13 @@ __global__ void collapse_write_kernel(const BvhNode* __restrict__ bin, const int
     for (int pass = 0; pass < 2; ++pass) {  // internal children, then leaves
         for (int j = 0; j < k; ++j) {
             if ((id[j] >= 0) != (pass == 0)) continue;
-            q.pl[0][slot] = lo[j].x;
-            q.pl[1][slot] = hi[j].x;
-            q.pl[2][slot] = lo[j].y;
-            q.pl[3][slot] = hi[j].y;
-            q.pl[4][slot] = lo[j].z;
-            q.pl[5][slot] = hi[j].z;
+            const float l3[3] = {lo[j].x, lo[j].y, lo[j].z}, h3[3] = {hi[j].x, hi[j].y, hi[j].z};
+            for (int a = 0; a < 3; ++a) {
+                q.pl[4 * a][slot] = l3[a];
+                q.pl[4 * a + 1][slot] = h3[a];
+                q.pl[4 * a + 2][slot] = h3[a];
+                q.pl[4 * a + 3][slot] = l3[a];
+            }
             if (id[j] < 0) {
                 q.child[slot] = id[j];
                 q.leaves |= 1u << slot;
@@ -532,7 +532,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     out.scene_r = upr(scene_r * 1.0001);
     out.o_max = down(o_max);
 
-    // Device buffers: the wide nodes + prims are kept; the rest (binary
+    // Device buffers: the 4-wide nodes + prims are kept; the rest (binary
     // nodes included) is build scratch.
     const size_t n_int = n >= 2 ? (size_t)n - 1 : 1;
     cudaError_t e = dev_malloc((void**)&out.prims, prims.size() * sizeof(float4));
@@ -606,7 +606,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
         // Karras tree, refit, then treelet restructuring passes (each pass
         // bottom-up; the leaves' starting parents are snapshot into keys, free
         // after the sort).  Restructuring can deepen the tree: should it pass
-        // the depth the wide traversal allows, the tree is rebuilt without.
+        // the depth the 4-wide traversal allows, the tree is rebuilt without.
         for (int passes = kRestructurePasses;; passes = 0) {
             karras_kernel<<<GI, B, 0, s>>>(keys2, vals2, (int)n, bin, parent_node, parent_leaf);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -631,14 +631,13 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
             if (depth <= 62 || passes == 0) break;
         }
 
-        // Collapse to wide nodes, one level per pass (count, scan, write): the
-        // greedy surface-area rule, or, should that tree be deeper than the
-        // traversal stack allows (kBvhMaxLevels, width - 1 entries each), the
-        // level rule (the binary tree is at most 63 deep: at most 32 levels at
-        // width 4, 21 at width 8).  At most n - 1 wide nodes (each holds >= 2
-        // children).
-        static_assert(kBvhMaxLevels >= (kBvhWidth == 8 ? 21 : 32), "stack too short for the level rule");
-        e = dev_malloc((void**)&out.nodes, n_int * sizeof(BvhWideNode));
+        // Collapse to 4-wide nodes, one level per pass (count, scan, write):
+        // the greedy surface-area rule, or, should that tree be deeper than
+        // the traversal stack allows (32 levels, 3 entries each), the level
+        // rule (the binary tree is at most 63 deep, so at most 32 levels).  At
+        // most n - 1 4-wide nodes (each holds >= 2 children).
+        static_assert(kBvhMaxLevels >= 32, "stack too short for the level rule");
+        e = dev_malloc((void**)&out.nodes, n_int * sizeof(Bvh4Node));
         if (e != cudaSuccess) return e;
         uint32_t m = 1, total = 1;
         for (int mode = 0; mode < 2; ++mode) {  // 0: greedy surface area, 1: level rule

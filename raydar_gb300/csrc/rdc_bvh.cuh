@@ -2,10 +2,10 @@
 //
 // The reference tests every object (src/renderer/cpu.rs:344-352).  For large
 // scenes the kernels instead walk a linear BVH: Morton-ordered objects, a
-// Karras (2012) radix tree of N-1 internal nodes, collapsed into a wide tree
-// (each node takes up to kBvhWidth binary descendants as its children): a
-// fraction of the dependent node loads per ray, that many independent box
-// tests per load.  The result must be the reference's exactly:
+// Karras (2012) radix tree of N-1 internal nodes, collapsed into a 4-wide
+// tree (each node takes up to four binary descendants as its children):
+// about half the dependent node loads per ray, four independent box tests per
+// node.  The result must be the reference's exactly:
 //   - leaves run the same exact sphere / cube tests as the brute-force loop;
 //   - the first-minimum rule (lowest object index among equal t) becomes a
 //     lexicographic minimum over (t, index), independent of visiting order;
@@ -41,35 +41,31 @@ struct alignas(16) BvhNode {
     float4 d;  // child 1 box max (xyz), 0
 };
 
-#ifndef RDC_BVH_WIDTH
-#define RDC_BVH_WIDTH 4
-#endif
-constexpr int kBvhWidth = RDC_BVH_WIDTH;  // children per node: 4 or 8
-static_assert(kBvhWidth == 4 || kBvhWidth == 8, "node width");
-
-// Wide node (kBvhWidth children; 128 bytes at 4, 256 at 8), its children's
-// boxes stored plane by plane:
-//   pl[0][j] min.x of child j   pl[1][j] max.x
-//   pl[2][j] min.y              pl[3][j] max.y
-//   pl[4][j] min.z              pl[5][j] max.z
-// For a positive direction component a box's near plane on that axis is its
-// minimum, for a negative one its maximum, so a ray reads the near planes of
-// all children on an axis with one load and the far planes with another,
-// from offsets fixed per ray: the box test needs no per-child min/max to
-// order the planes.  child[j]: >= 0 node, < 0 ~object; the internal children
-// take the first slots, at consecutive node indices from `first` (slot j's
-// node is first + j).  leaves: bit j set when slot j holds an object.  An
-// unused slot has min = +inf, max = -inf: every ray's near plane there is
-// +inf and its far plane -inf, so it is never entered.
-struct alignas(32) BvhWideNode {
-    float pl[6][kBvhWidth];
-    int child[kBvhWidth];
+// 4-wide node, 256 bytes.  For each axis a, 64 bytes of its children's box
+// planes: pl[4a][j] = min of child j, pl[4a + 1][j] = max, pl[4a + 2][j] =
+// max, pl[4a + 3][j] = min.  For a positive direction component a box's near
+// plane on that axis is its minimum, for a negative one its maximum, so a ray
+// reads the 32 bytes at 64a (positive) or 64a + 32 (negative) and has the
+// near planes of all four children in the first half and the far planes in
+// the second: one aligned 256-bit load per axis, one L1 access per lane, and
+// no per-child min/max to order the planes.  (Planes stored once, near and
+// far read with two 16-byte loads per axis, measured 11% slower: seven L1
+// accesses per visit instead of four, with the L1 data pipe the bound; 8-wide
+// nodes cut node visits per segment from 18.0 to 12.5 but cost 1.56x per
+// visit, 7% slower overall.)  child[j]: >= 0 node, < 0 ~object; the internal
+// children take the first slots, at consecutive node indices from `first`
+// (slot j's node is first + j).  leaves: bit j set when slot j holds an
+// object.  An unused slot has min = +inf, max = -inf: every ray's near plane
+// there is +inf and its far plane -inf, so it is never entered.
+constexpr int kBvhWidth = 4;
+struct alignas(32) Bvh4Node {
+    float pl[12][4];
+    int child[4];
     uint32_t leaves;
     int first;
-    uint32_t pad[kBvhWidth == 8 ? 6 : 2];
+    uint32_t pad[10];
 };
-static_assert(sizeof(BvhWideNode) == 32 * kBvhWidth, "wide node layout");
-constexpr uint32_t kPlaneBytes = 4 * kBvhWidth;  // one plane of every child
+static_assert(sizeof(Bvh4Node) == 256, "4-wide node layout");
 
 // BvhView (rdc_internal.hpp): nodes (root 0), prims (2 per object, scene
 // order: sphere (c, c.c) (r*r, 0, 0, kind); cube in the slab pair layout with
@@ -142,43 +138,28 @@ __device__ __forceinline__ void bvh_leaf(const BvhView& bv, const RayPre& r, int
 struct BvhRayBox {
     float inv[3];       // 1/d per axis
     float nn[3], nf[3]; // -(near origin term), -(far origin term) per axis
-    uint32_t near_off;  // byte offsets of the near planes: x in bits 0-7, y 8-15, z 16-23
+    uint32_t neg;       // sign bits of 1/d: x in bit 0, y 1, z 2
 };
-
-// One plane of every child (kBvhWidth floats) at byte offset off of node nb.
-__device__ __forceinline__ void ldg_planes(const char* nb, uint32_t off, float (&v)[kBvhWidth]) {
-    if constexpr (kBvhWidth == 8) {
-        float4 a, b;
-        ldg_pair(reinterpret_cast<const float4*>(nb + off), a, b);
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    } else {
-        const float4 a = __ldg(reinterpret_cast<const float4*>(nb + off));
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    }
-}
 
 // Entry (max(0, near)) of every child box, and a bit per child whose box is
 // entered no later than limit and left no earlier than 0.
-__device__ __forceinline__ unsigned bvh_boxes(const char* nb, const BvhRayBox& R, float limit,
-                                              float (&e)[kBvhWidth]) {
-    const uint32_t ox = R.near_off & 0xffu, oy = (R.near_off >> 8) & 0xffu, oz = R.near_off >> 16;
-    float nx[kBvhWidth], fx[kBvhWidth], ny[kBvhWidth], fy[kBvhWidth], nz[kBvhWidth], fz[kBvhWidth];
-    ldg_planes(nb, ox, nx);
-    ldg_planes(nb, ox ^ kPlaneBytes, fx);
-    ldg_planes(nb, oy, ny);
-    ldg_planes(nb, oy ^ kPlaneBytes, fy);
-    ldg_planes(nb, oz, nz);
-    ldg_planes(nb, oz ^ kPlaneBytes, fz);
+__device__ __forceinline__ unsigned bvh_boxes(const char* nb, const BvhRayBox& R, float limit, float (&e)[4]) {
+    float4 n[3], f[3];  // per axis: near planes of children 0-3, far planes
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        ldg_pair(reinterpret_cast<const float4*>(nb + 64 * a + ((R.neg >> a) & 1u) * 32u), n[a], f[a]);
+    const float nx[4] = {n[0].x, n[0].y, n[0].z, n[0].w}, fx[4] = {f[0].x, f[0].y, f[0].z, f[0].w};
+    const float ny[4] = {n[1].x, n[1].y, n[1].z, n[1].w}, fy[4] = {f[1].x, f[1].y, f[1].z, f[1].w};
+    const float nz[4] = {n[2].x, n[2].y, n[2].z, n[2].w}, fz[4] = {f[2].x, f[2].y, f[2].z, f[2].w};
     unsigned hits = 0u;
 #pragma unroll
-    for (int j = 0; j < kBvhWidth; ++j) {
-        const float n = fmax3(__fmaf_rn(nx[j], R.inv[0], R.nn[0]), __fmaf_rn(ny[j], R.inv[1], R.nn[1]),
-                              fmaxf(__fmaf_rn(nz[j], R.inv[2], R.nn[2]), 0.0f));
-        const float f = fmin3(__fmaf_rn(fx[j], R.inv[0], R.nf[0]), __fmaf_rn(fy[j], R.inv[1], R.nf[1]),
-                              fminf(__fmaf_rn(fz[j], R.inv[2], R.nf[2]), limit));
-        e[j] = n;
-        hits |= (n <= f ? 1u : 0u) << j;
+    for (int j = 0; j < 4; ++j) {
+        const float en = fmax3(__fmaf_rn(nx[j], R.inv[0], R.nn[0]), __fmaf_rn(ny[j], R.inv[1], R.nn[1]),
+                               fmaxf(__fmaf_rn(nz[j], R.inv[2], R.nn[2]), 0.0f));
+        const float ex = fmin3(__fmaf_rn(fx[j], R.inv[0], R.nf[0]), __fmaf_rn(fy[j], R.inv[1], R.nf[1]),
+                               fminf(__fmaf_rn(fz[j], R.inv[2], R.nf[2]), limit));
+        e[j] = en;
+        hits |= (en <= ex ? 1u : 0u) << j;
     }
     return hits;
 }
@@ -197,8 +178,8 @@ struct BvhTrav {
     unsigned lmask;      // the traversal is over when cur < 0 and lmask == 0
 };
 
-constexpr int kBvhStack = kBvhWidth == 8 ? 160 : 96;
-constexpr int kBvhMaxLevels = kBvhStack / (kBvhWidth - 1);  // 22 at width 8, 32 at width 4
+constexpr int kBvhStack = 96;
+constexpr int kBvhMaxLevels = kBvhStack / (kBvhWidth - 1);  // 32
 
 __device__ __forceinline__ void bvh_leaf_any(const BvhView& bv, const RayPre& r, bool fast, int obj, float& best,
                                              int& bidx) {
@@ -236,17 +217,17 @@ __device__ __forceinline__ void bvh_begin(const BvhView& bv, const RayPre& r, bo
     auto inv1 = [cap](float v, float rv) { return fabsf(v) * cap < 1.0f ? copysignf(cap, v) : rv; };
     const float iv[3] = {inv1(r.d.x, r.rd.x), inv1(r.d.y, r.rd.y), inv1(r.d.z, r.rd.z)};
     const float ov[3] = {r.o.x, r.o.y, r.o.z};
-    uint32_t off = 0;
+    uint32_t sg = 0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float oa = (ov[a] + m) * iv[a], ob = (ov[a] - m) * iv[a];
-        const bool neg = __float_as_uint(iv[a]) >> 31;  // near plane: the maximum (pl[2a + 1])
+        const bool neg = __float_as_uint(iv[a]) >> 31;  // near plane: the maximum
         T.box.inv[a] = iv[a];
         T.box.nn[a] = neg ? -ob : -oa;
         T.box.nf[a] = neg ? -oa : -ob;
-        off |= (2u * kPlaneBytes * a + (neg ? kPlaneBytes : 0u)) << (8 * a);
+        sg |= (neg ? 1u : 0u) << a;
     }
-    T.box.near_off = off;
+    T.box.neg = sg;
     T.cur = 0;
 }
 
@@ -295,29 +276,13 @@ __device__ __forceinline__ void bvh_cswap(uint32_t& a, uint32_t& b) {
     a = lo;
 }
 
-// Sort network on the visit's keys, ascending: 5 compare-exchanges for 4,
-// 19 for 8 (both halves, then Batcher's odd-even merge).
-__device__ __forceinline__ void bvh_sort4(uint32_t* k) {
+// Sort network on the visit's four keys, ascending (5 compare-exchanges).
+__device__ __forceinline__ void bvh_sort(uint32_t (&k)[4]) {
     bvh_cswap(k[0], k[1]);
     bvh_cswap(k[2], k[3]);
     bvh_cswap(k[0], k[2]);
     bvh_cswap(k[1], k[3]);
     bvh_cswap(k[1], k[2]);
-}
-__device__ __forceinline__ void bvh_sort(uint32_t (&k)[kBvhWidth]) {
-    bvh_sort4(k);
-    if constexpr (kBvhWidth == 8) {
-        bvh_sort4(k + 4);
-        bvh_cswap(k[0], k[4]);
-        bvh_cswap(k[1], k[5]);
-        bvh_cswap(k[2], k[6]);
-        bvh_cswap(k[3], k[7]);
-        bvh_cswap(k[2], k[4]);
-        bvh_cswap(k[3], k[5]);
-        bvh_cswap(k[1], k[2]);
-        bvh_cswap(k[3], k[4]);
-        bvh_cswap(k[5], k[6]);
-    }
 }
 
 // One node visit (T.cur >= 0, T.lmask == 0): the child boxes; leaf children
@@ -327,13 +292,13 @@ __device__ __forceinline__ void bvh_sort(uint32_t (&k)[kBvhWidth]) {
 // next stacked box still in front of the best hit, or none (T.cur = -1).
 // Internal children are ordered by a key per slot: the entry distance's bits
 // (non-negative: ordered as unsigned integers) with the low bits replaced by
-// the slot, at most 7 ulp off the entry; the stack keeps the entry rounded
-// down to a multiple of 8 ulp, so its test against the best hit stays
+// the slot, at most 3 ulp off the entry; the stack keeps the entry rounded
+// down to a multiple of 4 ulp, so its test against the best hit stays
 // conservative.
 template <class Stack>
 __device__ __forceinline__ void bvh_step(const BvhView& bv, const RayPre& r, bool fast, BvhTrav& T, Stack& stack,
                                          BvhCounters& cnt) {
-    const BvhWideNode* node = bv.nodes + checked_index(bv.oob, T.cur, bv.nnodes);
+    const Bvh4Node* node = bv.nodes + checked_index(bv.oob, T.cur, bv.nnodes);
     const char* nb = reinterpret_cast<const char*>(node);
     const uint2 meta = __ldg(reinterpret_cast<const uint2*>(&node->leaves));  // (leaves, first)
     ++cnt.visits;

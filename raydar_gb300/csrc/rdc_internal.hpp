@@ -53,12 +53,12 @@ struct SceneView {
     unsigned long long* oob;  // bounds-checked build: count of out-of-range indices caught
 };
 
-struct BvhWideNode;  // rdc_bvh.cuh
+struct Bvh4Node;  // rdc_bvh.cuh
 
-// Device LBVH of a scene (rdc_bvh.cu), collapsed to wide nodes (root 0),
+// Device LBVH of a scene (rdc_bvh.cu), collapsed to 4-wide nodes (root 0),
 // and 2 records per object in scene order.
 struct BvhView {
-    const BvhWideNode* nodes;
+    const Bvh4Node* nodes;
     const float4* prims;
     uint32_t nobj;
     float scene_r;  // bound on |centre| + size over the objects
@@ -68,8 +68,8 @@ struct BvhView {
 };
 
 struct BvhDevice {
-    BvhWideNode* nodes = nullptr;
-    uint32_t nnodes = 0;  // wide nodes
+    Bvh4Node* nodes = nullptr;
+    uint32_t nnodes = 0;  // 4-wide nodes
     float4* prims = nullptr;
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -81,8 +81,8 @@ struct BvhDevice {
 };
 
 // Build the LBVH of `sc` on stream `s` (synchronises it).  depth_out: the
-// deepest leaf of the binary tree (at most 63; the wide tree is at most
-// kBvhMaxLevels deep, so the traversal stack holds width - 1 entries per level).
+// deepest leaf of the binary tree (at most 63; the 4-wide tree is at most
+// 32 deep and its traversal stack holds 3 entries per level).
 cudaError_t build_lbvh(const struct rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s, uint32_t* depth_out);
 
 struct RenderParams {
