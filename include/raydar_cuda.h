@@ -403,6 +403,16 @@ rdc_status rdc_measure_fp32x2_issue(rdc_ctx* ctx, double* lane_ops_per_second);
  * the message a render would give; the context stays usable. */
 rdc_status rdc_selftest_staging_timeout(rdc_ctx* ctx);
 
+/* Self-tests of the device sort and prefix sum the LBVH build runs (no
+ * counterpart in the reference, which builds no hierarchy).  On n host
+ * values: rdc_selftest_radix_sort sorts the pairs (keys, vals) by key,
+ * stably, into keys_out / vals_out, for keys below 2^key_bits (key_bits
+ * 1..32; passes of 10 bits); rdc_selftest_exclusive_scan writes out[i] =
+ * in[0] + ... + in[i-1] (mod 2^32).  n <= RDC_MAX_OBJECTS. */
+rdc_status rdc_selftest_radix_sort(rdc_ctx* ctx, const uint32_t* keys, const uint32_t* vals, uint32_t n,
+                                   uint32_t key_bits, uint32_t* keys_out, uint32_t* vals_out);
+rdc_status rdc_selftest_exclusive_scan(rdc_ctx* ctx, const uint32_t* in, uint32_t n, uint32_t* out);
+
 /* ---- host-only helpers (no GPU needed) -------------------------------- */
 
 /* Recompute a camera's view, projection and inverse matrices from its

@@ -859,6 +859,71 @@ rdc_status rdc_selftest_staging_timeout(rdc_ctx* ctx) {
     return check_device_errors(ctx);
 }
 
+namespace {
+// Device buffers of a self-test, freed on every exit.
+struct SelftestBuffers {
+    std::vector<void*> p;
+    ~SelftestBuffers() {
+        for (void* q : p) cudaFree(q);
+    }
+    cudaError_t alloc(void** out, size_t bytes) {
+        *out = nullptr;
+        const cudaError_t e = rdc::dev_malloc(out, bytes > 0 ? bytes : 4);
+        if (e == cudaSuccess) p.push_back(*out);
+        return e;
+    }
+};
+}  // namespace
+
+rdc_status rdc_selftest_radix_sort(rdc_ctx* ctx, const uint32_t* keys, const uint32_t* vals, uint32_t n,
+                                   uint32_t key_bits, uint32_t* keys_out, uint32_t* vals_out) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!keys || !vals || !keys_out || !vals_out))
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_selftest_radix_sort: NULL argument");
+    if (key_bits < 1 || key_bits > 32)
+        return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_selftest_radix_sort: key_bits must be in 1..32");
+    if (n > RDC_MAX_OBJECTS) return fail(ctx, RDC_ERR_LIMIT, "rdc_selftest_radix_sort: n above RDC_MAX_OBJECTS");
+    if (rdc_status st = set_device(ctx)) return st;
+    if (n == 0) return RDC_OK;
+    SelftestBuffers b;
+    uint32_t *k0, *v0, *k1, *v1;
+    void* scratch;
+    const size_t bytes = (size_t)n * 4;
+    RDC_CUDA(ctx, b.alloc((void**)&k0, bytes));
+    RDC_CUDA(ctx, b.alloc((void**)&v0, bytes));
+    RDC_CUDA(ctx, b.alloc((void**)&k1, bytes));
+    RDC_CUDA(ctx, b.alloc((void**)&v1, bytes));
+    RDC_CUDA(ctx, b.alloc(&scratch, rdc::radix_sort_scratch_bytes(n)));
+    RDC_CUDA(ctx, cudaMemcpyAsync(k0, keys, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(v0, vals, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    uint32_t *ks = nullptr, *vs = nullptr;
+    RDC_CUDA(ctx, rdc::radix_sort_pairs(k0, v0, k1, v1, n, (int)key_bits, scratch, ctx->stream, &ks, &vs));
+    RDC_CUDA(ctx, cudaMemcpyAsync(keys_out, ks, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(vals_out, vs, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RDC_OK;
+}
+
+rdc_status rdc_selftest_exclusive_scan(rdc_ctx* ctx, const uint32_t* in, uint32_t n, uint32_t* out) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!in || !out)) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_selftest_exclusive_scan: NULL argument");
+    if (n > RDC_MAX_OBJECTS) return fail(ctx, RDC_ERR_LIMIT, "rdc_selftest_exclusive_scan: n above RDC_MAX_OBJECTS");
+    if (rdc_status st = set_device(ctx)) return st;
+    if (n == 0) return RDC_OK;
+    SelftestBuffers b;
+    uint32_t *d_in, *d_out;
+    void* scratch;
+    const size_t bytes = (size_t)n * 4;
+    RDC_CUDA(ctx, b.alloc((void**)&d_in, bytes));
+    RDC_CUDA(ctx, b.alloc((void**)&d_out, bytes));
+    RDC_CUDA(ctx, b.alloc(&scratch, rdc::exclusive_scan_scratch_bytes(n)));
+    RDC_CUDA(ctx, cudaMemcpyAsync(d_in, in, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    RDC_CUDA(ctx, rdc::exclusive_scan(d_in, d_out, n, scratch, ctx->stream));
+    RDC_CUDA(ctx, cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    RDC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RDC_OK;
+}
+
 rdc_status rdc_measure_fp32x2_issue(rdc_ctx* ctx, double* lane_ops_per_second) {
     if (!ctx || !lane_ops_per_second)
         return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_measure_fp32x2_issue: NULL argument");

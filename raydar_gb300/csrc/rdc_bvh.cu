@@ -3,7 +3,7 @@
 //   1. object boxes and primitive records (host, exact reference constants)
 //   2. 30-bit Morton code of each box centre in the cube spanning the scene's
 //      centre bounds
-//   3. radix sort of (code, object) pairs (CUB)
+//   3. stable radix sort of (code, object) pairs (rdc_sort.cu)
 //   4. Karras, "Maximizing parallelism in the construction of BVHs, octrees
 //      and k-d trees" (HPG 2012): internal node i of N-1 finds its key range
 //      and split from the longest common prefixes of (code, position) keys
@@ -20,7 +20,7 @@
 //      starts from its binary node's two children and opens the internal
 //      child of largest surface area until it has four (a greedy surface-area
 //      collapse); nodes are numbered level by level through a prefix sum
-//      (CUB), so the layout is deterministic and every node's internal
+//      (rdc_sort.cu), so the layout is deterministic and every node's internal
 //      children have consecutive indices.  If that tree would be deeper than
 //      the traversal stack allows, every internal child is opened once
 //      instead (each node takes its binary node's grandchildren), which
@@ -30,9 +30,6 @@
 #include <cstring>
 #include <string>
 #include <vector>
-
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
 
 #include "raydar_cuda.h"
 #include "rdc_bvh.cuh"
@@ -536,12 +533,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     // nodes included) is build scratch.
     const size_t n_int = n >= 2 ? (size_t)n - 1 : 1;
     cudaError_t e = dev_malloc((void**)&out.prims, prims.size() * sizeof(float4));
-    size_t sort_tmp = 0, scan_tmp = 0;
-    if (e == cudaSuccess)
-        e = cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                            (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30, s);
-    if (e == cudaSuccess)
-        e = cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n_int, s);
+    const size_t sort_tmp = radix_sort_scratch_bytes(n), scan_tmp = exclusive_scan_scratch_bytes((uint32_t)n_int);
     // scratch: box (2n float4) | binary nodes (n-1) | keys, keys2, vals, vals2 (4n u32) | parents (2n int) |
     //          flags, counts, map (3n u32) | two collapse frontiers (n-1 int2 each) | depth | sort tmp | scan tmp
     const size_t box_b = 2 * (size_t)n * sizeof(float4);
@@ -598,8 +590,15 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
     const uint32_t B = 256, G = (n + B - 1) / B;
     morton_kernel<<<G, B, 0, s>>>(d_box, n, lo, inv_ext, keys, vals);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    e = cub::DeviceRadixSort::SortPairs(d_sort, sort_tmp, keys, keys2, vals, vals2, (int)n, 0, 30, s);
-    if (e != cudaSuccess) return e;
+    {
+        uint32_t *ks = nullptr, *vs = nullptr;
+        e = radix_sort_pairs(keys, vals, keys2, vals2, n, 30, d_sort, s, &ks, &vs);
+        if (e != cudaSuccess) return e;
+        if (ks != keys2) {  // the sorted pairs are in (keys2, vals2) from here on
+            std::swap(keys, keys2);
+            std::swap(vals, vals2);
+        }
+    }
     uint32_t depth = 1;
     if (n >= 2) {
         const uint32_t GI = (uint32_t)((n_int + B - 1) / B);
@@ -652,7 +651,7 @@ cudaError_t build_lbvh(const rdc_scene_desc* sc, BvhDevice& out, cudaStream_t s,
                 const uint32_t GM = (m + B - 1) / B;
                 collapse_count_kernel<<<GM, B, 0, s>>>(bin, front, m, mode != 0, counts);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
-                e = cub::DeviceScan::ExclusiveSum(d_scan, scan_tmp, counts, map, (int)m, s);
+                e = exclusive_scan(counts, map, m, d_scan, s);
                 if (e != cudaSuccess) return e;
                 collapse_write_kernel<<<GM, B, 0, s>>>(bin, front, m, mode != 0, map, total, out.nodes, front_next);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;

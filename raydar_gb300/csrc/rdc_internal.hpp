@@ -80,6 +80,18 @@ struct BvhDevice {
     BvhView view(unsigned long long* oob) const { return BvhView{nodes, prims, nobj, scene_r, o_max, nnodes, oob}; }
 };
 
+// Device sort and prefix sum (rdc_sort.cu).  radix_sort_pairs sorts the n
+// pairs (keys, vals) by the low key_bits bits of the keys, stably, using
+// (keys_alt, vals_alt) as the second buffer; the sorted arrays are whichever
+// pair *keys_sorted / *vals_sorted name.  exclusive_scan: out[i] = in[0] +
+// ... + in[i-1], n <= 2^24, out == in allowed.  Scratch of the stated sizes.
+size_t radix_sort_scratch_bytes(uint32_t n);
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t n,
+                             int key_bits, void* scratch, cudaStream_t s, uint32_t** keys_sorted,
+                             uint32_t** vals_sorted);
+size_t exclusive_scan_scratch_bytes(uint32_t n);
+cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, void* scratch, cudaStream_t s);
+
 // Build the LBVH of `sc` on stream `s` (synchronises it).  depth_out: the
 // deepest leaf of the binary tree (at most 63; the 4-wide tree is at most
 // 32 deep and its traversal stack holds 3 entries per level).

@@ -133,6 +133,9 @@ SIGNATURES = {
     "rdc_measure_fp32_issue": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "rdc_measure_fp32x2_issue": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "rdc_selftest_staging_timeout": (C.c_int, [_P]),
+    "rdc_selftest_radix_sort": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
+                                          C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "rdc_selftest_exclusive_scan": (C.c_int, [_P, C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint32)]),
     "rdc_camera_update_matrices": (C.c_int, [C.POINTER(RdcCamera)]),
 }
 

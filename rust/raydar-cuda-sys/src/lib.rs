@@ -199,6 +199,10 @@ extern "C" {
                                   -> rdc_status;
     pub fn rdc_measure_fp32x2_issue(ctx: *mut rdc_ctx, lane_ops_per_second: *mut f64) -> rdc_status;
     pub fn rdc_selftest_staging_timeout(ctx: *mut rdc_ctx) -> rdc_status;
+    pub fn rdc_selftest_radix_sort(ctx: *mut rdc_ctx, keys: *const u32, vals: *const u32, n: u32, key_bits: u32,
+                                   keys_out: *mut u32, vals_out: *mut u32) -> rdc_status;
+    pub fn rdc_selftest_exclusive_scan(ctx: *mut rdc_ctx, input: *const u32, n: u32, out: *mut u32)
+                                       -> rdc_status;
 
     // host only
     pub fn rdc_camera_update_matrices(camera: *mut rdc_camera) -> rdc_status;
