@@ -169,9 +169,12 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_baseline(w, seconds: float):
+def cpu_baseline(w, seconds: float, gpu=None):
     """The oracle on one host thread over a random pixel sample of the same
-    1080p workload (1 spp, 12 bounces), sized to about `seconds` of work."""
+    1080p workload (1 spp, 12 bounces), sized to about `seconds` of work.
+    With `gpu` (a CudaRenderer holding the same scene), the last sample's
+    pixels are compared with the GPU's render of the same seed and sample:
+    the images are matched when they are bit-identical (RMSE 0)."""
     import numpy as np
 
     import oracle
@@ -179,11 +182,12 @@ def cpu_baseline(w, seconds: float):
     npix = w.scene.width * w.scene.height
     rng = np.random.default_rng(0)
     n = 2000
+    seed = 7
     total_seg, total_t, total_px = 0, 0.0, 0
     while True:
         px = rng.choice(npix, n, replace=False).astype(np.uint32)
         t0 = time.perf_counter()
-        _, seg = oracle.render_pixels(sc, px, 0, 1, w.max_bounces, 7)
+        acc, seg = oracle.render_pixels(sc, px, 0, 1, w.max_bounces, seed)
         dt = time.perf_counter() - t0
         total_seg += seg
         total_t += dt
@@ -192,10 +196,23 @@ def cpu_baseline(w, seconds: float):
             break
         rate = max(n / max(dt, 1e-6), 1.0)
         n = int(min(npix, max(500, rate * (seconds - total_t) * 1.05)))
-    return {"value": total_seg / total_t, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{total_px} random pixels of the 1920x1080 c2_default frame, 1 spp, "
-                      f"{w.max_bounces} bounces, {total_seg} segments in {total_t:.1f} s "
-                      f"(CPU oracle, -O3 -ffp-contract=off, one thread)"}
+    out = {"value": total_seg / total_t, "unit": UNIT, "cores": 1, "kind": "port",
+           "sample": f"{total_px} random pixels of the 1920x1080 c2_default frame, 1 spp, "
+                     f"{w.max_bounces} bounces, {total_seg} segments in {total_t:.1f} s "
+                     f"(CPU oracle, -O3 -ffp-contract=off, one thread)"}
+    if gpu is not None:
+        gpu.seed = seed
+        gpu._check(gpu.lib.rdc_reset(gpu.ctx), "rdc_reset")
+        gpu.render_range(0, 1)
+        g = gpu.accumulator(w.scene).reshape(-1, 4)[px]
+        rgb_g, rgb_c = g[:, :3].astype(np.float64), acc[:, :3].astype(np.float64)
+        out["image_check"] = {
+            "pixels": int(len(px)),
+            "bit_identical": bool(g.tobytes() == acc.tobytes()),
+            "rmse_gpu_vs_cpu": float(np.sqrt(((rgb_g - rgb_c) ** 2).mean())),
+            "what": "the CPU sample's last batch of pixels against the GPU render of the same seed and sample",
+        }
+    return out
 
 
 # --------------------------------------------------------------- reference --
@@ -814,7 +831,7 @@ def run_ours(args):
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:
-        base = cpu_baseline(w, args.cpu_seconds)
+        base = cpu_baseline(w, args.cpu_seconds, gpu=r)
 
     r.close()
     if dist is not None:
