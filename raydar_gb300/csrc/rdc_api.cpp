@@ -1159,6 +1159,7 @@ rdc_status rdc_batch_upload(rdc_ctx* ctx, const rdc_batch_item* items, uint32_t 
         bs.key0 = (uint32_t)items[i].seed;
         bs.key1 = (uint32_t)(items[i].seed >> 32);
         bs.work_begin = (float)(acc_work / total_work);
+        bs.pixel_work = bs.npix ? (float)(work[i] / total_work / (double)bs.npix * 1e6) : 0.0f;
         acc_work += work[i];
         if (bs.spp == 0) bs.npix = 0;  // nothing to render: the pool starts empty
     }

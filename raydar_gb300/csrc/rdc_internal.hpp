@@ -186,6 +186,7 @@ struct BatchScene {
     uint32_t key0;
     uint32_t key1;
     float work_begin;  // cumulative estimated work before this scene, in [0, 1)
+    float pixel_work;  // estimated work of one pixel (relative)
 };
 
 struct BatchParams {

@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kRenderBvhBlock, 5) render_bvh_kernel(const Re
 // pixel for all of the scene's samples).  Blocks start on scenes in
 // proportion to each scene's estimated work; a block whose scene pool is
 // empty waits for its warps to finish their pixels, then moves to the scene
-// with the most pixels left.  RNG stream = batch index.
+// with pixels left whose pixels cost most.  RNG stream = batch index.
 __device__ __forceinline__ int batch_initial_scene(const BatchParams& P, float pos, int lane) {
     int count = 0;  // scenes whose work starts at or before pos
     for (uint32_t base = 0; base < P.nscenes; base += 32) {
@@ -253,8 +253,12 @@ __device__ __forceinline__ int batch_initial_scene(const BatchParams& P, float p
     return count > 0 ? count - 1 : 0;
 }
 
-// The scene with the most pixels not yet handed out (lowest index on ties),
-// or -1 when every pool is empty.  Called by one full warp.
+// Of the scenes with pixels not yet handed out, the one whose pixels are
+// estimated to cost most (lowest index on ties), or -1 when every pool is
+// empty: expensive pixels go first, so the batch ends on cheap ones (measured
+// +1% scenes/s on config 3 over the scene with most pixels left; starting
+// every block on the most expensive scene instead of in proportion to each
+// scene's work, 9% slower).  Called by one full warp.
 __device__ __forceinline__ int batch_busiest_scene(const BatchParams& P, int lane) {
     uint32_t best = 0;
     int best_s = -1;
@@ -262,8 +266,11 @@ __device__ __forceinline__ int batch_busiest_scene(const BatchParams& P, int lan
         const uint32_t taken = *reinterpret_cast<volatile const uint32_t*>(&P.pixel_counters[s]);
         const uint32_t npix = P.scenes[s].npix;
         const uint32_t left = taken < npix ? npix - taken : 0u;
-        if (left > best) {
-            best = left;
+        // a non-negative float's bits order like its value; | 1 keeps a scene
+        // with pixels left (and a zero estimate) above the empty ones
+        const uint32_t key = left ? __float_as_uint(P.scenes[s].pixel_work) | 1u : 0u;
+        if (key > best) {
+            best = key;
             best_s = (int)s;
         }
     }
