@@ -599,16 +599,13 @@ def progressive_bench(local: int, samples: int = 256, size: int = 584, bounces: 
     }
 
 
-def wavefront_bench(local: int, steps: int, spp: int = 64):
-    """Megakernel vs wavefront A/B on the headline scene (c2_default 1920x1080,
-    12 bounces) at `spp` samples per frame: the same paths, the same
-    accumulator bit for bit; device time of each form."""
-    from raydar_gb300 import CudaRenderer, RendererConfig, scenegen
-
-    w = scenegen.c2_default()
+def _mk_vs_wf(local, w, spp, steps, accel=None):
+    from raydar_gb300 import CudaRenderer, RendererConfig
     out = {}
     for fn in ("rdc_render", "rdc_render_wavefront"):
         r = CudaRenderer(RendererConfig(max_bounces=w.max_bounces), device=local, seed=0)
+        if accel is not None:
+            r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
         r.upload(w.scene)
         f = getattr(r.lib, fn)
         r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
@@ -623,11 +620,27 @@ def wavefront_bench(local: int, steps: int, spp: int = 64):
             segs += st.segments
         r.close()
         out[fn] = {"ms_per_frame": ms / steps, "segments_per_s": segs / (ms / 1e3)}
-    mk, wf = out["rdc_render"], out["rdc_render_wavefront"]
+    return out["rdc_render"], out["rdc_render_wavefront"]
+
+
+def wavefront_bench(local: int, steps: int, spp: int = 64, lbvh_spp: int = 16):
+    """Megakernel vs wavefront A/B on the headline scene (c2_default 1920x1080,
+    12 bounces) at `spp` samples per frame, and on the config-5 LBVH scene
+    (1920x1080, 12 bounces) at `lbvh_spp`: the same paths, the same
+    accumulator bit for bit; device time of each form."""
+    from raydar_gb300 import native, scenegen
+
+    mk, wf = _mk_vs_wf(local, scenegen.c2_default(), spp, steps)
+    lmk, lwf = _mk_vs_wf(local, scenegen.c5_large(), lbvh_spp, steps, accel=native.ACCEL_LBVH)
     return {
         "workload": f"c2_default 1920x1080, {spp} spp per frame, 12 bounces, 81 objects",
         "megakernel": mk, "wavefront": wf,
         "wavefront_over_megakernel_time": wf["ms_per_frame"] / mk["ms_per_frame"],
+        "lbvh": {
+            "workload": f"c5_large 1920x1080, {lbvh_spp} spp per frame, 12 bounces, 110k objects, device LBVH",
+            "megakernel": lmk, "wavefront": lwf,
+            "wavefront_over_megakernel_time": lwf["ms_per_frame"] / lmk["ms_per_frame"],
+        },
         "steps": steps,
     }
 

@@ -316,8 +316,10 @@ rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* 
  * (diffuse/specular mix, metal, glass, miss) so each warp shades one class.
  * One wave is one sample of every pixel (a CUDA graph replayed per sample),
  * which keeps the per-pixel sample order of src/renderer/cpu.rs:198-210.
- * Brute-force scenes only (RDC_ERR_UNSUPPORTED with an LBVH).  Provided for
- * the megakernel / wavefront comparison; rdc_render is the faster form. */
+ * With an LBVH the closest hits come from a persistent kernel whose lanes
+ * take queued rays as they finish their traversals (refill_min_idle of
+ * rdc_set_render_config sets how many idle lanes trigger a refill).
+ * Provided for the megakernel / wavefront comparison. */
 rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces,
                                 uint64_t seed);
 

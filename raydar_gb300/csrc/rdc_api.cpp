@@ -639,8 +639,9 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
         return fail(ctx, RDC_ERR_LIMIT, "rdc_render_wavefront: max_bounces above RDC_MAX_BOUNCES");
     if ((uint64_t)spp_begin + spp_count > 0xFFFFFFFFull)
         return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_render_wavefront: sample range overflows 32 bits");
-    if (ctx->bvh_active || !ctx->brute_fits)
-        return fail(ctx, RDC_ERR_UNSUPPORTED, "rdc_render_wavefront: brute-force scenes only (no LBVH)");
+    if (!ctx->bvh_active && !ctx->brute_fits)
+        return fail(ctx, RDC_ERR_LIMIT,
+                    "rdc_render_wavefront: brute force needs the scene's records in shared memory; use the LBVH");
     if (rdc_status st = set_device(ctx)) return st;
     const uint32_t npix = ctx->width * ctx->height;
     ctx->last_paths = (uint64_t)npix * spp_count;
@@ -668,6 +669,11 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     p.sample = ctx->d_wf_counts + 6;
     p.segments = ctx->d_counters + 1;
     p.errors = ctx->d_counters + kErrorCounter;
+    p.use_bvh = ctx->bvh_active ? 1u : 0u;
+    p.bvh = ctx->bvh_active ? ctx->bvh.view(ctx->d_counters + kBoundsCounter)
+                            : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f, 0, nullptr};
+    p.bvh_counters = ctx->d_counters + 2;
+    p.min_idle = ctx->render_cfg.refill_min_idle;
     float* f = reinterpret_cast<float*>(ctx->d_wf);
     float** planes[12] = {&p.ox, &p.oy, &p.oz, &p.dx, &p.dy, &p.dz, &p.ar, &p.ag, &p.ab, &p.lr, &p.lg, &p.lb};
     for (int i = 0; i < 12; ++i) *planes[i] = f + (size_t)i * npix;
@@ -677,9 +683,9 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     p.queue0 = u;
     p.queue1 = u + npix;
     p.cls = u + 2 * (size_t)npix;
-    const size_t smem = rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
+    const size_t smem = ctx->bvh_active ? 0 : rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
     int per_i = 0, per_s = 0;
-    RDC_CUDA(ctx, rdc::wavefront_occupancy(256, smem, &per_i, &per_s));
+    RDC_CUDA(ctx, rdc::wavefront_occupancy(ctx->bvh_active, 256, smem, &per_i, &per_s));
     if (per_i < 1 || per_s < 1) return fail(ctx, RDC_ERR_LIMIT, "rdc_render_wavefront: kernels do not fit on an SM");
     const int grid_i = ctx->num_sms * per_i, grid_s = ctx->num_sms * per_s;
     RDC_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));

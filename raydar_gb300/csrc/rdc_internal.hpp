@@ -166,12 +166,21 @@ struct WfParams {
     int* hit_obj;
     uint32_t *queue0, *queue1;  // ray queues (pixel ids), alternating per bounce
     uint32_t* cls;              // 4 class queues of npix entries: mix, metal, glass, miss
-    uint32_t* counts;           // [0], [1] ray queue lengths, [2..5] class queue lengths
+    uint32_t* counts;           // [0], [1] ray queue lengths, [2..5] class queue lengths, [6] the
+                                // wave's sample index, [7] the LBVH intersect kernel's fetch counter
     unsigned long long* segments;
     unsigned long long* errors;  // device errors (shared-memory staging that did not complete)
+    uint32_t use_bvh;            // 1: the LBVH intersect kernel over bvh, 0: brute force
+    BvhView bvh;
+    unsigned long long* bvh_counters;  // node visits, object tests (LBVH)
+    uint32_t min_idle;           // LBVH intersect: idle lanes of a warp before it refills
 };
+constexpr int kWfBvhBlock = 128;      // wf_intersect_bvh: threads per block
+constexpr int kWfBvhMinBlocks = 6;    // and the resident blocks its registers are sized for (80; 8 blocks at
+                                      // 64 registers measured 5% slower)
 size_t wavefront_state_bytes(uint32_t npix);
-cudaError_t wavefront_occupancy(int block, size_t smem, int* intersect_per_sm, int* shade_per_sm);
+size_t wavefront_bvh_smem_bytes();
+cudaError_t wavefront_occupancy(bool bvh, int block, size_t smem, int* intersect_per_sm, int* shade_per_sm);
 cudaError_t wavefront_set_sample(uint32_t* sample, uint32_t v, cudaStream_t s);
 cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s);
 

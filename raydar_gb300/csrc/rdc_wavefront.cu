@@ -21,6 +21,7 @@
 // by the accumulate kernel.  Results are bit-identical to render_kernel.
 #include <cstdint>
 
+#include "rdc_bvh.cuh"
 #include "rdc_device.cuh"
 
 namespace rdc {
@@ -98,6 +99,123 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
     if (lane == 0 && s != 0ull) atomicAdd(P.segments, s);
+}
+
+// Append the lanes with cls >= 0 (their pixel pix) to the class queues,
+// one warp-aggregated atomic per class present.  Called by a full warp.
+__device__ __forceinline__ void wf_append_class(const WfParams& P, int cls, uint32_t pix) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const unsigned m = __ballot_sync(FULL, cls == c);
+        if (m == 0u) continue;
+        const int leader = __ffs(m) - 1;
+        uint32_t b = 0;
+        if (lane == leader) b = atomicAdd(&P.counts[2 + c], (uint32_t)__popc(m));
+        b = __shfl_sync(FULL, b, leader);
+        if (cls == c)
+            P.cls[(size_t)c * P.npix + checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npix)] = pix;
+    }
+}
+
+// LBVH scenes: the closest hit of every queued ray through the device LBVH,
+// by a persistent grid whose lanes fetch rays from the queue as they finish
+// (one warp-aggregated atomic per refill).  Each lane runs render_bvh_kernel's
+// traversal state machine; a loop iteration is a node visit (up to two) or a
+// deferred leaf test, whichever more lanes wait for, until min_idle lanes are
+// done; then the finished lanes store their hit, append their pixel to a
+// class queue and take the next rays.  There is no shading in this kernel, so
+// a refill costs only the ray set-up, and a lane holds only traversal state.
+__global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
+    wf_intersect_bvh(const WfParams P, const uint32_t* __restrict__ q_in, const uint32_t* __restrict__ n_in,
+                     uint32_t* __restrict__ fetch) {
+    extern __shared__ uint2 s_stack[];  // kShortStack entries per thread
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint2 deep[kBvhStack - kShortStack];
+    SplitStack stack{s_stack + threadIdx.x, blockDim.x, deep};
+    const uint32_t n = *n_in;
+    const bool scene_fast = P.sc.fast_div != 0u;
+    BvhCounters cnt;
+    BvhTrav T;
+    T.cur = -1;
+    T.lmask = 0u;
+    T.best = 0.0f;
+    T.bidx = -1;
+    RayPre r;
+    bool rfast = false, busy = false, pool_open = true;
+    uint32_t pix = 0, segs = 0;
+    for (;;) {
+        // lanes whose traversal is over: store the hit, queue the pixel by class
+        const bool done = busy && T.cur < 0 && T.lmask == 0u;
+        int cls = -1;
+        if (done) {
+            P.hit_t[pix] = T.best;
+            P.hit_obj[pix] = T.bidx;
+            if (T.bidx < 0) {
+                cls = 3;
+            } else {
+                const MatDev* mp = P.sc.mat + checked_index(P.sc.oob, T.bidx, P.sc.nobj);
+                const float metallic = __ldg(&mp->b.w), transmission = __ldg(&mp->c.x);
+                cls = transmission > 0.0f ? 2 : (metallic >= 1.0f ? 1 : 0);  // material_class
+            }
+            busy = false;
+        }
+        if (__ballot_sync(FULL, done) != 0u) wf_append_class(P, cls, pix);
+        // refill the idle lanes from the ray queue
+        const unsigned idle = __ballot_sync(FULL, !busy);
+        if (idle != 0u && pool_open) {
+            const unsigned c = (unsigned)__popc(idle);
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, c);
+            base = __shfl_sync(FULL, base, leader);
+            if (base + c >= n) pool_open = false;
+            if (!busy) {
+                const uint32_t mine = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (mine < n) {
+                    pix = (uint32_t)checked_index(P.sc.oob, q_in[mine], P.npix);
+                    const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
+                    const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
+                    r = ray_pre(o, d, P.sc.neg_zero);
+                    rfast = scene_fast && r.fast;
+                    bvh_begin(P.bvh, r, rfast, T, cnt);
+                    busy = true;
+                    ++segs;
+                }
+            }
+        }
+        if (__ballot_sync(FULL, busy) == 0u && !pool_open) break;
+        // traversal steps until min_idle lanes are done (at least one step)
+        for (bool first = true;; first = false) {
+            const bool wl = busy && T.lmask != 0u;
+            const bool wn = busy && T.lmask == 0u && T.cur >= 0;
+            const unsigned lm = __ballot_sync(FULL, wl), nm = __ballot_sync(FULL, wn);
+            const unsigned act = lm | nm;
+            if (act == 0u || (!first && 32u - (unsigned)__popc(act) >= P.min_idle)) break;
+            if (__popc(lm) >= __popc(nm)) {
+                if (wl) bvh_leaf_step(P.bvh, r, rfast, T, cnt);
+            } else if (wn) {
+                bvh_step(P.bvh, r, rfast, T, stack, cnt);
+                if (T.lmask == 0u && T.cur >= 0) bvh_step(P.bvh, r, rfast, T, stack, cnt);
+            }
+        }
+    }
+    unsigned long long s2 = segs;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s2 += __shfl_down_sync(FULL, s2, off);
+    if (lane == 0 && s2 != 0ull) atomicAdd(P.segments, s2);
+    unsigned long long v = cnt.visits, t = cnt.tests;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v += __shfl_down_sync(FULL, v, off);
+        t += __shfl_down_sync(FULL, t, off);
+    }
+    if (lane == 0 && P.bvh_counters) {
+        if (v) atomicAdd(P.bvh_counters, v);
+        if (t) atomicAdd(P.bvh_counters + 1, t);
+    }
 }
 
 __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounce, uint32_t* __restrict__ q_out,
@@ -183,10 +301,19 @@ size_t wavefront_state_bytes(uint32_t npix) {
     return (size_t)npix * 4u * 20u;
 }
 
-cudaError_t wavefront_occupancy(int block, size_t smem, int* intersect_per_sm, int* shade_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(wf_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(intersect_per_sm, wf_intersect, block, smem);
+size_t wavefront_bvh_smem_bytes() { return (size_t)kWfBvhBlock * kShortStack * sizeof(uint2); }
+
+cudaError_t wavefront_occupancy(bool bvh, int block, size_t smem, int* intersect_per_sm, int* shade_per_sm) {
+    cudaError_t e = cudaSuccess;
+    if (bvh) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(intersect_per_sm, wf_intersect_bvh, kWfBvhBlock,
+                                                          wavefront_bvh_smem_bytes());
+    } else {
+        e = cudaFuncSetAttribute(wf_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(smem < 48 * 1024 ? 48 * 1024 : smem));
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(intersect_per_sm, wf_intersect, block, smem);
+    }
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(shade_per_sm, wf_shade, block, 0);
     return e;
 }
@@ -197,7 +324,8 @@ cudaError_t wavefront_set_sample(uint32_t* sample, uint32_t v, cudaStream_t s) {
 }
 
 // Enqueue one wave (one sample of every pixel) on s; captured into a graph by
-// the caller.  grid_i / grid_s: persistent grids of the two queue kernels.
+// the caller.  grid_i / grid_s: persistent grids of the two queue kernels
+// (the intersect kernel is wf_intersect_bvh when p.use_bvh).
 cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s) {
     const uint32_t b = 256, g = (p.npix + b - 1) / b;
     wf_generate<<<g, b, 0, s>>>(p);
@@ -209,8 +337,12 @@ cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem,
         uint32_t* n_out = p.counts + ((bounce + 1u) & 1u);
         e = cudaMemsetAsync(n_out, 0, sizeof(uint32_t), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(p.counts + 2, 0, 4 * sizeof(uint32_t), s);
+        if (e == cudaSuccess && p.use_bvh) e = cudaMemsetAsync(p.counts + 7, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) break;
-        wf_intersect<<<grid_i, 256, smem, s>>>(p, q_in, n_in);
+        if (p.use_bvh)
+            wf_intersect_bvh<<<grid_i, kWfBvhBlock, wavefront_bvh_smem_bytes(), s>>>(p, q_in, n_in, p.counts + 7);
+        else
+            wf_intersect<<<grid_i, 256, smem, s>>>(p, q_in, n_in);
         e = cudaGetLastError();
         if (e != cudaSuccess) break;
         wf_shade<<<grid_s, 256, 0, s>>>(p, bounce, q_out, n_out);

@@ -4,7 +4,8 @@ device array (materials, hit records, LBVH nodes and primitives, accumulators,
 dL/dimage, gradient rows, wavefront queues) is range-checked; an index out of
 range is counted and reported as RDC_ERR_DEVICE, never trapped.  A subprocess
 runs every kernel family through the checked library -- brute-force renders,
-the reference's benchmark scene, the LBVH, the wavefront form, a batch, the
+the reference's benchmark scene, the LBVH, the wavefront form (brute force
+and LBVH), a batch, the
 adjoint on both accelerations, the single-stage checks and the allocation-
 free render -- and must see no device error and the oracle's results."""
 import json
@@ -63,6 +64,7 @@ run("brute", lambda: render("brute", c1, 2, 8, 5))
 run("benchmark_scene", lambda: render("benchmark_scene", bench, 1, 12, 6))
 run("lbvh", lambda: render("lbvh", big, 1, 6, 9, accel=native.ACCEL_LBVH))
 run("wavefront", lambda: render("wavefront", c2, 2, 12, 7, wavefront=True))
+run("wavefront_lbvh", lambda: render("wavefront_lbvh", big, 2, 8, 14, accel=native.ACCEL_LBVH, wavefront=True))
 
 def batch():
     items = [(c1, 2, 6, 11), (resized(scenegen.c1_plain(seed=4).scene, 16, 16), 1, 4, 12)]
@@ -143,6 +145,8 @@ def test_checked_renders_equal_the_oracle(checked_run):
         ("benchmark_scene", resized(Scene.load(GOLDEN / "benchmark.rscn"), 48, 27), 1, 12, 6, 0),
         ("lbvh", scenegen.c5_large(seed=3, width=24, height=16, n_spheres=600, n_cubes=60).scene, 1, 6, 9, 0),
         ("wavefront", resized(scenegen.c2_default().scene, 32, 18), 2, 12, 7, 0),
+        ("wavefront_lbvh", scenegen.c5_large(seed=3, width=24, height=16, n_spheres=600, n_cubes=60).scene,
+         2, 8, 14, 0),
         ("batch0", c1, 2, 6, 11, 0), ("batch1", resized(scenegen.c1_plain(seed=4).scene, 16, 16), 1, 4, 12, 1),
     ]
     for name, scene, spp, bounces, seed, stream in cases:

@@ -10,10 +10,12 @@ from tests.helpers import bits_equal, shrink
 pytestmark = pytest.mark.gpu
 
 
-def _both(scene, s0, n, bounces, seed):
+def _both(scene, s0, n, bounces, seed, accel=None):
     out = []
     for fn in ("rdc_render", "rdc_render_wavefront"):
         r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
+        if accel is not None:
+            r._check(r.lib.rdc_set_accel(r.ctx, accel), "set_accel")
         r.upload(scene)
         r._check(r.lib.rdc_reset(r.ctx), "reset")
         r._check(getattr(r.lib, fn)(r.ctx, s0, n, bounces, seed), fn)
@@ -41,10 +43,37 @@ def test_wavefront_progressive_and_zero_bounces():
     assert sa == sb == 0 and bits_equal(a, b) and np.all(b[..., 3] == 2)
 
 
-def test_wavefront_refuses_lbvh_scenes():
-    scene = shrink(scenegen.c2_default().scene, 32, 18)
-    r = CudaRenderer(RendererConfig(), seed=1)
-    r._check(r.lib.rdc_set_accel(r.ctx, native.ACCEL_LBVH), "set_accel")
-    r.upload(scene)
-    assert r.lib.rdc_render_wavefront(r.ctx, 0, 1, 4, 1) == 2  # RDC_ERR_UNSUPPORTED
-    r.close()
+def test_wavefront_lbvh_equals_megakernel_lbvh_and_the_oracle():
+    """LBVH scenes take the persistent LBVH intersect kernel: the same
+    accumulator as the LBVH megakernel and the oracle's brute force."""
+    import oracle
+    scene = scenegen.c5_large(seed=4, width=40, height=24, n_spheres=3000, n_cubes=300).scene
+    (a, sa), (b, sb) = _both(scene, 0, 3, 12, 21, accel=native.ACCEL_LBVH)
+    assert sa == sb
+    assert bits_equal(a, b)
+    ref, segs = oracle.render(scene.to_c(), 0, 3, 12, 21, threads=8)
+    assert segs == sb and bits_equal(b, ref)
+
+
+def test_wavefront_lbvh_on_small_scenes_and_refill_thresholds():
+    """One object (no tree nodes), a forced LBVH on a config scene, and
+    refill thresholds from 1 to 32: all bit-identical to the megakernel."""
+    one = shrink(scenegen.c1_plain().scene, 24, 16)
+    one.objects = one.objects[:1]
+    (a, sa), (b, sb) = _both(one, 0, 2, 6, 3, accel=native.ACCEL_LBVH)
+    assert sa == sb and bits_equal(a, b)
+    scene = shrink(scenegen.c2_default().scene, 48, 27)
+    ref = None
+    for mi in (1, 8, 16, 32):
+        r = CudaRenderer(RendererConfig(max_bounces=12), seed=8)
+        r._check(r.lib.rdc_set_accel(r.ctx, native.ACCEL_LBVH), "set_accel")
+        cfg = native.RdcLaunchConfig(256, 0, mi)
+        r._check(r.lib.rdc_set_render_config(r.ctx, native.C.byref(cfg)), "cfg")
+        r.upload(scene)
+        r._check(r.lib.rdc_reset(r.ctx), "reset")
+        r._check(r.lib.rdc_render_wavefront(r.ctx, 0, 2, 12, 8), "wavefront")
+        acc = r.accumulator(scene)
+        r.close()
+        if ref is None:
+            (ref, _), _ = _both(scene, 0, 2, 12, 8, accel=native.ACCEL_LBVH)
+        assert bits_equal(acc, ref), mi
