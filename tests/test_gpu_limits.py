@@ -7,7 +7,9 @@
 - RDC_MAX_BOUNCES (1024): paths that never escape a closed box run all their
   bounces, brute force and LBVH, bit-identical to the oracle;
 - RDC_MAX_BRUTE_OBJECTS (4096): brute force at the limit, its refusal one
-  object above it, and the LBVH on the same scenes.
+  object above it, and the LBVH on the same scenes;
+- RDC_MAX_OBJECTS (2^24): the LBVH build and traversal against the oracle's
+  brute force on a ray sample.
 """
 import numpy as np
 import pytest
@@ -105,3 +107,24 @@ def test_brute_force_refuses_one_object_above_its_limit():
     ref, segs = oracle.render(scene.to_c(), 0, 1, 4, 2, threads=16)
     acc, st = _render(scene, 1, 4, 2, native.ACCEL_AUTO)
     assert st.accel == native.ACCEL_LBVH and st.segments == segs and bits_equal(acc, ref)
+
+
+def test_lbvh_at_the_object_limit():
+    """RDC_MAX_OBJECTS (2^24) objects in the config-5 volume: the device
+    build (its radix sort and prefix sums at their largest) and the traversal
+    give the brute-force closest hit of the oracle on a ray sample."""
+    from tests.test_gpu_bvh import _intersect, _ray_sample
+    n_obj = 1 << 24
+    w = scenegen.c5_large(seed=24, width=64, height=36, n_spheres=n_obj - (1 << 20), n_cubes=1 << 20)
+    r = CudaRenderer(RendererConfig(), seed=0)
+    r._check(r.lib.rdc_set_accel(r.ctx, native.ACCEL_LBVH), "set_accel")
+    r.upload(w.scene)
+    st = r.stats()
+    assert st.accel == native.ACCEL_LBVH and 0 < st.bvh_depth <= 64
+    o, d = _ray_sample(w.scene, w.scene.packed, 24, np.random.default_rng(24))  # the oracle: ~0.4 s a ray
+    got = _intersect(r, o, d)
+    r.close()
+    ref = oracle.intersect(w.scene.to_c(), o, d)
+    for g, e in zip(got, ref):
+        assert bits_equal(g, e)
+    assert (got[1] >= 0).sum() > 12  # most rays hit something in a volume this dense
