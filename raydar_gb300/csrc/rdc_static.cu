@@ -199,7 +199,7 @@ extern "C" rdc_status rdc_render_static(const rdc_scene_desc* sc, float* accum_d
     if (e != cudaSuccess) return cuda_error(error_out, error_capacity, e, "cudaMemsetAsync(counters)");
 
     if (spp_count > 0) {
-        rdc::RenderParams p;
+        rdc::RenderParams p{};  // fields the brute-force kernel does not read stay zero
         rdc::SceneView& v = p.sc;
         v.rec = d_rec;
         v.nrec = fc.nrec;
