@@ -92,3 +92,55 @@ def test_random_scene_matches_the_oracle(k):
         acc, s = _gpu(scene, spp, bounces, seed, accel, wf)
         assert s == segs, (accel, wf)
         assert bits_equal(acc, ref), (k, accel, wf, len(scene.objects))
+
+
+@pytest.mark.parametrize("k", range(12))
+def test_random_batch_matches_the_oracle(k):
+    """A batch of 2-9 random scenes in one persistent launch: each equals the
+    oracle's render with RNG stream = its batch index."""
+    from raydar_gb300.batch import BatchRenderer
+    rng = np.random.default_rng(5000 + k)
+    items = []
+    for j in range(int(rng.integers(2, 10))):
+        scene, spp, bounces = _random_scene(20000 + 37 * k + j)
+        items.append((scene, spp, bounces, 900 + 13 * k + j))
+    br = BatchRenderer(items)
+    try:
+        br.render()
+        total = br.stats().segments
+        seg_sum = 0
+        for i, (sc, spp, bounces, seed) in enumerate(items):
+            ref, seg = oracle.render(sc.to_c(), 0, spp, bounces, seed, threads=8, stream=i)
+            assert bits_equal(br.accumulator(i), ref), (k, i)
+            seg_sum += seg
+        assert total == seg_sum
+    finally:
+        br.close()
+
+
+@pytest.mark.parametrize("k", range(24))
+def test_random_scene_adjoint_matches_the_fp64_oracle(k):
+    """rdc_backward on random scenes (1-16 bounces, both accelerations)
+    against the FP64 gradient oracle over the same paths, within the relative
+    L2 error of 1e-2 the gradients are specified with.  (dL/dimage is uniform
+    in [-1, 1], so an object's gradient is a sum of terms of both signs; the
+    FP32 atomic sums carry a rounding error relative to the terms' magnitudes,
+    which a sum that cancels can show as ~1e-3 of the total: measured up to
+    1.8e-3 on these scenes.)"""
+    scene, spp, _ = _random_scene(40000 + k)
+    bounces = int(np.random.default_rng(k).choice([1, 3, 6, 16]))
+    seed = 300 + k
+    dl = np.random.default_rng(60 + k).uniform(-1, 1, (scene.height, scene.width, 3)).astype(np.float32)
+    oa, orr, oe, _ = oracle.gradient(scene.to_c(), 0, spp, bounces, seed, dl, threads=8)
+    for accel in (native.ACCEL_BRUTE_FORCE, native.ACCEL_LBVH):
+        r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
+        try:
+            r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
+            r.forward(scene, spp)
+            ga, gr, ge = r.backward(scene, dl)
+        finally:
+            r.close()
+        for name, g, o in (("albedo", ga, oa), ("roughness", gr, orr), ("emission", ge, oe)):
+            no = float(np.linalg.norm(o))
+            err = float(np.linalg.norm(np.asarray(g, np.float64) - o))
+            assert err <= 1e-2 * no + 1e-6, (k, accel, name, err, no)
