@@ -19,7 +19,7 @@ from tests.helpers import bits_equal
 
 pytestmark = pytest.mark.gpu
 
-N_SCENES = 300
+N_SCENES = 1000
 
 
 def _random_scene(seed):
@@ -66,6 +66,28 @@ def _random_scene(seed):
     return Scene(cam, world, objs), spp, bounces
 
 
+def _extreme_scene(seed):
+    """Coordinates from 1e-4 to 1e7, object sizes from 1e-5 to 1e5 and cameras
+    far from them: the fast paths' range guards and the IEEE fallbacks, and the
+    LBVH's rounding-bound box growth, at their edges."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    scale = float(rng.choice([1e-4, 1e-2, 1.0, 1e3, 1e5, 1e7]))
+    n = int(rng.choice([1, 5, 40, 200]))
+    objs = []
+    for i in range(n):
+        c = (rng.normal(size=3) * scale).astype(f32)
+        size = float(f32(scale * np.exp(rng.uniform(np.log(1e-5), np.log(1.0)))))
+        m = Material(albedo=rng.uniform(0, 1, 3).astype(f32), roughness=float(f32(rng.uniform())),
+                     metallic=float(f32(rng.choice([0.0, 1.0]))), transmission=float(f32(rng.choice([0.0, 1.0]))))
+        objs.append(Object("Sphere" if rng.random() < 0.6 else "Cube", c, size, m))
+    pos = (rng.normal(size=3) * scale * float(rng.choice([0.5, 3.0, 100.0]))).astype(f32)
+    tgt = (rng.normal(size=3) * scale * 0.2).astype(f32)
+    cam = Camera.new(pos, tgt, [0.0, 1.0, 0.0], 24, 16, 0.01, 1000.0, fov=float(rng.uniform(10, 100)))
+    world = World("SkyColor", rng.uniform(0, 1, 3).astype(f32), rng.uniform(0, 1, 3).astype(f32))
+    return Scene(cam, world, objs), int(rng.integers(1, 3)), int(rng.choice([1, 4, 12]))
+
+
 def _gpu(scene, spp, bounces, seed, accel, wavefront=False):
     r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
     try:
@@ -92,6 +114,17 @@ def test_random_scene_matches_the_oracle(k):
         acc, s = _gpu(scene, spp, bounces, seed, accel, wf)
         assert s == segs, (accel, wf)
         assert bits_equal(acc, ref), (k, accel, wf, len(scene.objects))
+
+
+@pytest.mark.parametrize("k", range(200))
+def test_extreme_scale_scene_matches_the_oracle(k):
+    scene, spp, bounces = _extreme_scene(7000 + k)
+    seed = 11 + k
+    ref, segs = oracle.render(scene.to_c(), 0, spp, bounces, seed, threads=8)
+    for accel in (native.ACCEL_LBVH, native.ACCEL_BRUTE_FORCE):
+        acc, s = _gpu(scene, spp, bounces, seed, accel)
+        assert s == segs, (k, accel)
+        assert bits_equal(acc, ref), (k, accel, len(scene.objects))
 
 
 @pytest.mark.parametrize("k", range(12))
