@@ -320,17 +320,13 @@ __global__ void __launch_bounds__(kRenderBlock, kShRec ? RDC_ADJ_SH_MIN_BLOCKS :
                     idx = (int)checked_index(P.sc.oob, idx, P.sc.nobj);
                     const MatDev m = load_mat(P.sc.mat, idx);
                     const HitRec h = closest_hit(o, d, t, __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
-                    uint32_t w[12];
                     const uint32_t c2 = b * 4u;
-                    const U4 w0 = philox(pix, sample, c2, P.stream_id, P.key0, P.key1);
-                    const U4 w1 = philox(pix, sample, c2 + 1u, P.stream_id, P.key0, P.key1);
-                    const U4 w2 = philox(pix, sample, c2 + 2u, P.stream_id, P.key0, P.key1);
-                    w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
-                    w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
-                    w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
                     ScatterRec rec;
                     V3 no, nd;
-                    scatter_impl<true>(d, h, m, w, no, nd, &rec);
+                    scatter_lobe_first<true>(d, h, m, philox(pix, sample, c2, P.stream_id, P.key0, P.key1),
+                                             philox(pix, sample, c2 + 1u, P.stream_id, P.key0, P.key1),
+                                             philox(pix, sample, c2 + 2u, P.stream_id, P.key0, P.key1), no, nd,
+                                             &rec);
                     AdjVert& vk = v[nv++];
                     vk.o = o;
                     vk.d = d;

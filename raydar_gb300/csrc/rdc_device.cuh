@@ -31,7 +31,7 @@ __device__ __forceinline__ U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint
             k0 += 0x9E3779B9u;
             k1 += 0xBB67AE85u;
         }
-        const uint32_t lo0 = 0xD2511F53u * c0;
+const uint32_t lo0 = 0xD2511F53u * c0;
         const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
         const uint32_t lo1 = 0xCD9E8D57u * c2;
         const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
@@ -596,44 +596,44 @@ struct ScatterRec {
     V3 s;
 };
 
-// The hit branch of per_pixel (src/renderer/cpu.rs:262-328): new ray from a
-// hit, the object's material and the bounce's random words w[0..10].  With
-// Rec, also fills *rec; the arithmetic is the same either way.
+// The hit branch of per_pixel (src/renderer/cpu.rs:262-328): the new ray
+// from a hit, the object's material and the bounce's random words, lobe
+// first.  The reference builds both the diffuse and the specular candidate
+// direction and keeps one of them (or the refracted one); only the kept
+// direction's arithmetic reaches the new ray, so deciding the lobe from the
+// coin words first and building that direction alone gives the same bits
+// with one unit-sphere vector and one or two normalisations instead of two
+// and three (measured +1.4% on the 81-object brute-force frame, +1.7%
+// through the LBVH).  a, b and q are the bounce's three Philox blocks (words
+// 0-3, 4-7, 8-11).  With Rec, also fills *rec for the adjoint's replay (the
+// flip bit is set for the diffuse lobe only, the one lobe that reads it).
+// (Drawing q only for the lanes that read it -- the roughness coin inside
+// (0, 1) and the refracted lobe -- measured 2.5% slower on the brute-force
+// frame: a warp's lanes rarely all skip it, and the branch costs more than
+// the block.)
 template <bool Rec>
-__device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev& m, const uint32_t* w, V3& o_out,
-                                             V3& d_out, ScatterRec* rec) {
+__device__ __forceinline__ void scatter_lobe_first(V3 d, const HitRec& h, const MatDev& m, const U4 a, const U4 b,
+                                                   const U4 q, V3& o_out, V3& d_out, ScatterRec* rec) {
     const float rough = m.a.w;
     const float metallic = m.b.w;
     const float transmission = m.c.x;
-
-    V3 diffuse = vadd(h.n, unit_sphere(w[0], w[1], w[2]));
-    const bool flip = vdot(diffuse, h.n) < 0.0f;
-    if (flip) diffuse = vneg(diffuse);
-
-    // reflect, src/utils/mod.rs:14-16: v - n * (v.n) * 2
-    const float dn = vdot(d, h.n);
-    const V3 perfect = vsub(d, vmul(vmul(h.n, dn), 2.0f));
-    const V3 s2 = unit_sphere(w[3], w[4], w[5]);
-    const V3 specular = vnormalize(vadd(perfect, vmul(s2, rough)));
-    uint32_t lobe = kLobeSpecular;
+    const bool trans = u01(b.z) < transmission;  // word 6
+    bool refracted = false, diffuse = false;
     uint32_t coin = 0u;
-    V3 s_used = s2;
-
-    const bool trans = u01(w[6]) < transmission;
-    V3 dir;
+    float ratio = 0.0f, cos_theta = 0.0f;
+    V3 rd = h.n;
     if (trans) {
-        const float ratio = h.front ? m.c.y : m.c.z;
+        ratio = h.front ? m.c.y : m.c.z;
         const float r0 = h.front ? m.c.w : m.d.x;
-        const V3 rd = vnormalize(d);
+        rd = vnormalize(d);
         const V3 nn = vneg(h.n);
-        const float cos_theta = fminf(vdot(rd, nn), 1.0f);
+        cos_theta = fminf(vdot(rd, nn), 1.0f);
         const float mm = 1.0f - cos_theta;
         const float m2 = mm * mm;
         const float m5 = mm * (m2 * m2);
         const float refl = r0 + (1.0f - r0) * m5;
-        bool refracted = false;
-        const bool coin_refracts = refl < u01(w[7]);
-        if (coin_refracts || Rec) {  // the recording form also needs it when the coin says reflect
+        const bool coin_refracts = refl < u01(b.w);  // word 7
+        if (coin_refracts || Rec) {  // the record also needs can_refract when the coin says reflect
             // can_refract, src/utils/mod.rs:37-44
             const float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
             const bool can = ratio * sin_theta <= 1.0f;
@@ -641,42 +641,62 @@ __device__ __forceinline__ void scatter_impl(V3 d, const HitRec& h, const MatDev
             // under total internal reflection the lobe is reflection whatever the coin says
             coin = can ? kScatFresnelCoin : 0u;
         }
+    } else if (!(u01(b.w) < metallic)) {  // word 7
+        diffuse = u01(q.x) < rough;          // word 8
+        coin = kScatRoughCoin;
+    }
+    // the lobe's unit-sphere vector: words 0-2 (diffuse), 8-10 (refracted), 3-5 (specular)
+    const uint32_t ua = diffuse ? a.x : refracted ? q.x : a.w;
+    const uint32_t ub = diffuse ? a.y : refracted ? q.y : b.x;
+    const uint32_t uc = diffuse ? a.z : refracted ? q.z : b.y;
+    const V3 sv = unit_sphere(ua, ub, uc);
+    V3 dir;
+    bool flip = false;
+    if (diffuse) {
+        dir = vadd(h.n, sv);
+        flip = vdot(dir, h.n) < 0.0f;
+        if (flip) dir = vneg(dir);
+    } else {
+        V3 base;
         if (refracted) {
             // refract, src/utils/mod.rs:25-35
             const V3 perp = vmul(vadd(rd, vmul(h.n, cos_theta)), ratio);
-            const float s = -sqrtf(fabsf(1.0f - vdot(perp, perp)));
-            const V3 rf = vadd(perp, vmul(h.n, s));
-            const V3 s3 = unit_sphere(w[8], w[9], w[10]);
-            dir = vnormalize(vadd(rf, vmul(s3, rough)));
-            lobe = kLobeRefract;
-            s_used = s3;
+            const float sq = -sqrtf(fabsf(1.0f - vdot(perp, perp)));
+            base = vadd(perp, vmul(h.n, sq));
         } else {
-            dir = specular;
+            // reflect, src/utils/mod.rs:14-16: v - n * (v.n) * 2
+            const float dn = vdot(d, h.n);
+            base = vsub(d, vmul(vmul(h.n, dn), 2.0f));
         }
-    } else if (u01(w[7]) < metallic) {
-        dir = specular;
-    } else if (u01(w[8]) < rough) {
-        dir = diffuse;
-        lobe = kLobeDiffuse;
-        coin = kScatRoughCoin;
-    } else {
-        dir = specular;
-        coin = kScatRoughCoin;
+        dir = vnormalize(vadd(base, vmul(sv, rough)));
     }
     const V3 off = trans ? dir : h.n;
     o_out = vadd(h.p, vmul(off, 0.0001f));
     const bool to_normal = vdot(dir, dir) < 1e-10f;
     d_out = to_normal ? h.n : dir;
     if (Rec) {
+        const uint32_t lobe = diffuse ? kLobeDiffuse : refracted ? kLobeRefract : kLobeSpecular;
         rec->flags = lobe | (flip ? kScatFlip : 0u) | (trans ? kScatTrans : 0u) | (to_normal ? kScatNormal : 0u) |
                      (h.front ? kScatFront : 0u) | coin;
-        rec->s = s_used;
+        rec->s = sv;
     }
 }
 
+// The scatter from twelve given words.
 __device__ __forceinline__ void scatter(V3 d, const HitRec& h, const MatDev& m, const uint32_t* w, V3& o_out,
                                         V3& d_out) {
-    scatter_impl<false>(d, h, m, w, o_out, d_out, nullptr);
+    scatter_lobe_first<false>(d, h, m, U4{w[0], w[1], w[2], w[3]}, U4{w[4], w[5], w[6], w[7]},
+                              U4{w[8], w[9], w[10], w[11]}, o_out, d_out, nullptr);
+}
+
+// One bounce's scatter with its random words drawn from the Philox blocks
+// (pix, sample, c2 .. c2 + 2, stream).
+__device__ __forceinline__ void scatter_drawn(V3 d, const HitRec& h, const MatDev& m, uint32_t pix, uint32_t sample,
+                                              uint32_t c2, uint32_t stream_id, uint32_t k0, uint32_t k1, V3& o_out,
+                                              V3& d_out) {
+    scatter_lobe_first<false>(d, h, m, philox(pix, sample, c2, stream_id, k0, k1),
+                              philox(pix, sample, c2 + 1u, stream_id, k0, k1),
+                              philox(pix, sample, c2 + 2u, stream_id, k0, k1), o_out, d_out, nullptr);
 }
 
 // World::sample, src/scene/world.rs:17-31 (the dot with +Y is d.x*0 + d.y*1 + d.z*0).
@@ -863,16 +883,8 @@ __device__ __forceinline__ bool segment_shade(const SceneView& sc, PathState& s,
     const float4 hi = __ldg(&sc.hit[ci]);
     const MatDev m = load_mat(sc.mat, ci);
     const HitRec h = closest_hit(s.o, s.d, t, hi, __float_as_int(m.d.y));
-    uint32_t w[12];
-    const uint32_t c2 = s.bounce * 4u;
-    const U4 w0 = philox(pix, sample, c2, stream_id, k0, k1);
-    const U4 w1 = philox(pix, sample, c2 + 1u, stream_id, k0, k1);
-    const U4 w2 = philox(pix, sample, c2 + 2u, stream_id, k0, k1);
-    w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
-    w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
-    w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
     V3 no, nd;
-    scatter(s.d, h, m, w, no, nd);
+    scatter_drawn(s.d, h, m, pix, sample, s.bounce * 4u, stream_id, k0, k1, no, nd);
     s.o = no;
     s.d = nd;
     s.atten = mk(s.atten.x * m.a.x, s.atten.y * m.a.y, s.atten.z * m.a.z);

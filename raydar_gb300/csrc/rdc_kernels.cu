@@ -212,14 +212,17 @@ __global__ void __launch_bounds__(kRenderBvhBlock, 5) render_bvh_kernel(const Re
         if (__ballot_sync(FULL, pix >= 0) == 0u) break;
         // Traversal until min_idle lanes are done (at least one step).  Each
         // step is a node visit for the lanes without pending leaves, or a
-        // leaf test for the lanes with some, whichever more lanes wait for.
+        // leaf test for the lanes with some, whichever more lanes wait for;
+        // leaf lanes count twice, as a node step makes up to two visits
+        // (measured +0.7% over an even vote; 3:1 equal, 4:1 and 8:1 slower,
+        // 1:2 -4%).
         for (bool first = true;; first = false) {
             const bool wl = in_flight && T.lmask != 0u;
             const bool wn = in_flight && T.lmask == 0u && T.cur >= 0;
             const unsigned lm = __ballot_sync(FULL, wl), nm = __ballot_sync(FULL, wn);
             const unsigned act = lm | nm;
             if (act == 0u || (!first && 32u - (unsigned)__popc(act) >= P.min_idle)) break;
-            if (__popc(lm) >= __popc(nm)) {
+            if (2 * __popc(lm) >= __popc(nm)) {
                 if (wl) bvh_leaf_step(P.bvh, r, rfast, T, cnt);
             } else if (wn) {
                 // up to two node visits per iteration (a lane with no leaves

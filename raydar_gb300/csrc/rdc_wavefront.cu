@@ -194,7 +194,8 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
             const unsigned lm = __ballot_sync(FULL, wl), nm = __ballot_sync(FULL, wn);
             const unsigned act = lm | nm;
             if (act == 0u || (!first && 32u - (unsigned)__popc(act) >= P.min_idle)) break;
-            if (__popc(lm) >= __popc(nm)) {
+            // leaf lanes count twice, as in the megakernel (+0.6% here)
+            if (2 * __popc(lm) >= __popc(nm)) {
                 if (wl) bvh_leaf_step(P.bvh, r, rfast, T, cnt);
             } else if (wn) {
                 bvh_step(P.bvh, r, rfast, T, stack, cnt);
@@ -249,16 +250,8 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
                 const int idx = (int)checked_index(P.sc.oob, P.hit_obj[pix], P.sc.nobj);
                 const MatDev m = load_mat(P.sc.mat, idx);
                 const HitRec h = closest_hit(o, d, P.hit_t[pix], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
-                uint32_t w[12];
-                const uint32_t c2w = bounce * 4u;
-                const U4 w0 = philox(pix, sample, c2w, P.stream_id, P.key0, P.key1);
-                const U4 w1 = philox(pix, sample, c2w + 1u, P.stream_id, P.key0, P.key1);
-                const U4 w2 = philox(pix, sample, c2w + 2u, P.stream_id, P.key0, P.key1);
-                w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
-                w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
-                w[8] = w2.x; w[9] = w2.y; w[10] = w2.z; w[11] = w2.w;
                 V3 no, nd;
-                scatter(d, h, m, w, no, nd);
+                scatter_drawn(d, h, m, pix, sample, bounce * 4u, P.stream_id, P.key0, P.key1, no, nd);
                 P.ox[pix] = no.x; P.oy[pix] = no.y; P.oz[pix] = no.z;
                 P.dx[pix] = nd.x; P.dy[pix] = nd.y; P.dz[pix] = nd.z;
                 atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
