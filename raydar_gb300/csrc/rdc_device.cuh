@@ -31,7 +31,7 @@ __device__ __forceinline__ U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint
             k0 += 0x9E3779B9u;
             k1 += 0xBB67AE85u;
         }
-const uint32_t lo0 = 0xD2511F53u * c0;
+        const uint32_t lo0 = 0xD2511F53u * c0;
         const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
         const uint32_t lo1 = 0xCD9E8D57u * c2;
         const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
