@@ -81,7 +81,7 @@ struct rdc_ctx {
     // wavefront render (rdc_render_wavefront)
     char* d_wf = nullptr;
     size_t cap_wf = 0;
-    uint32_t* d_wf_counts = nullptr;  // 6 queue lengths + the wave's sample index
+    uint32_t* d_wf_counts = nullptr;  // queue lengths, the wave's first sample and sample count
     cudaGraphExec_t wf_exec = nullptr;
 
     // differentiation (rdc_forward / rdc_backward)
@@ -654,19 +654,26 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
         cudaGraphExecDestroy(ctx->wf_exec);
         ctx->wf_exec = nullptr;
     }
-    if (rdc_status st = ensure(ctx, &ctx->d_wf, &ctx->cap_wf, rdc::wavefront_state_bytes(npix), "wavefront state"))
+    static_assert((uint64_t)RDC_MAX_RESOLUTION * RDC_MAX_RESOLUTION <= (1ull << rdc::kWfPixBits),
+                  "a queue entry holds any pixel index");
+    static_assert(rdc::kWfMaxWaveSpp <= (1u << (32 - rdc::kWfPixBits)), "and any place in a wave");
+    const uint32_t wave = rdc::wavefront_wave_spp(npix, spp_count, ctx->bvh_active);
+    const uint32_t npath = npix * wave;
+    if (rdc_status st = ensure(ctx, &ctx->d_wf, &ctx->cap_wf, rdc::wavefront_state_bytes(npath), "wavefront state"))
         return st;
-    if (!ctx->d_wf_counts) RDC_CUDA(ctx, rdc::dev_malloc((void**)&ctx->d_wf_counts, 8 * sizeof(uint32_t)));
+    if (!ctx->d_wf_counts) RDC_CUDA(ctx, rdc::dev_malloc((void**)&ctx->d_wf_counts, 16 * sizeof(uint32_t)));
     rdc::WfParams p;
     p.sc = ctx->view;
     p.accum = ctx->d_accum;
     p.npix = npix;
+    p.npath = npath;
     p.max_bounces = max_bounces;
     p.stream_id = 0;
     p.key0 = (uint32_t)seed;
     p.key1 = (uint32_t)(seed >> 32);
     p.counts = ctx->d_wf_counts;
     p.sample = ctx->d_wf_counts + 6;
+    p.wave_n = ctx->d_wf_counts + 8;
     p.segments = ctx->d_counters + 1;
     p.errors = ctx->d_counters + kErrorCounter;
     p.use_bvh = ctx->bvh_active ? 1u : 0u;
@@ -676,13 +683,13 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     p.min_idle = ctx->render_cfg.refill_min_idle;
     float* f = reinterpret_cast<float*>(ctx->d_wf);
     float** planes[12] = {&p.ox, &p.oy, &p.oz, &p.dx, &p.dy, &p.dz, &p.ar, &p.ag, &p.ab, &p.lr, &p.lg, &p.lb};
-    for (int i = 0; i < 12; ++i) *planes[i] = f + (size_t)i * npix;
-    p.hit_t = f + (size_t)12 * npix;
-    p.hit_obj = reinterpret_cast<int*>(f + (size_t)13 * npix);
-    uint32_t* u = reinterpret_cast<uint32_t*>(f + (size_t)14 * npix);
+    for (int i = 0; i < 12; ++i) *planes[i] = f + (size_t)i * npath;
+    p.hit_t = f + (size_t)12 * npath;
+    p.hit_obj = reinterpret_cast<int*>(f + (size_t)13 * npath);
+    uint32_t* u = reinterpret_cast<uint32_t*>(f + (size_t)14 * npath);
     p.queue0 = u;
-    p.queue1 = u + npix;
-    p.cls = u + 2 * (size_t)npix;
+    p.queue1 = u + npath;
+    p.cls = u + 2 * (size_t)npath;
     const size_t smem = ctx->bvh_active ? 0 : rdc::render_smem_bytes(ctx->view.nrec, ctx->view.nruns);
     int per_i = 0, per_s = 0;
     RDC_CUDA(ctx, rdc::wavefront_occupancy(ctx->bvh_active, 256, smem, &per_i, &per_s));
@@ -699,12 +706,17 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     e = cudaGraphInstantiate(&ctx->wf_exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
-    RDC_CUDA(ctx, rdc::wavefront_set_sample(p.sample, spp_begin, ctx->stream));
+    RDC_CUDA(ctx, rdc::wavefront_set_word(p.sample, spp_begin, ctx->stream));
+    RDC_CUDA(ctx, rdc::wavefront_set_word(p.wave_n, wave, ctx->stream));
+    const uint32_t nwaves = (spp_count + wave - 1) / wave, last = spp_count - (nwaves - 1) * wave;
     RDC_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-    for (uint32_t k = 0; k < spp_count; ++k) RDC_CUDA(ctx, cudaGraphLaunch(ctx->wf_exec, ctx->stream));
+    for (uint32_t k = 0; k < nwaves; ++k) {
+        if (k + 1 == nwaves && last != wave) RDC_CUDA(ctx, rdc::wavefront_set_word(p.wave_n, last, ctx->stream));
+        RDC_CUDA(ctx, cudaGraphLaunch(ctx->wf_exec, ctx->stream));
+    }
     RDC_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->last_timed = true;
-    ctx->last_launches = spp_count * (2u + 2u * max_bounces);
+    ctx->last_launches = nwaves * (2u + 2u * max_bounces) + (last != wave ? 1u : 0u);
     ctx->sample_count = spp_begin + spp_count > ctx->sample_count ? spp_begin + spp_count : ctx->sample_count;
     return RDC_OK;
 }

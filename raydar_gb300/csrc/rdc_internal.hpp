@@ -159,15 +159,18 @@ struct WfParams {
     SceneView sc;
     float4* accum;
     uint32_t npix, max_bounces, stream_id, key0, key1;
-    uint32_t* sample;   // the wave's sample index (device), advanced per wave
-    float *ox, *oy, *oz, *dx, *dy, *dz;  // the path's next ray
+    uint32_t npath;     // paths a wave holds: npix x the wave's sample capacity W
+    uint32_t* sample;   // the wave's first sample index (device), advanced per wave
+    uint32_t* wave_n;   // samples in the current wave (device), W or the remainder in the last
+    float *ox, *oy, *oz, *dx, *dy, *dz;  // the path's next ray (npath entries each)
     float *ar, *ag, *ab, *lr, *lg, *lb;  // throughput, radiance
     float* hit_t;
     int* hit_obj;
-    uint32_t *queue0, *queue1;  // ray queues (pixel ids), alternating per bounce
-    uint32_t* cls;              // 4 class queues of npix entries: mix, metal, glass, miss
+    uint32_t *queue0, *queue1;  // ray queues of path entries, alternating per bounce
+    uint32_t* cls;              // 4 class queues of npath entries: mix, metal, glass, miss
     uint32_t* counts;           // [0], [1] ray queue lengths, [2..5] class queue lengths, [6] the
-                                // wave's sample index, [7] the LBVH intersect kernel's fetch counter
+                                // wave's first sample index, [7] the LBVH intersect kernel's fetch
+                                // counter, [8] the wave's sample count
     unsigned long long* segments;
     unsigned long long* errors;  // device errors (shared-memory staging that did not complete)
     uint32_t use_bvh;            // 1: the LBVH intersect kernel over bvh, 0: brute force
@@ -178,10 +181,20 @@ struct WfParams {
 constexpr int kWfBvhBlock = 128;      // wf_intersect_bvh: threads per block
 constexpr int kWfBvhMinBlocks = 6;    // and the resident blocks its registers are sized for (80; 8 blocks at
                                       // 64 registers measured 5% slower)
-size_t wavefront_state_bytes(uint32_t npix);
+constexpr uint32_t kWfPixBits = 28;          // a queue entry: the path's place in its wave << 28 | its pixel
+constexpr uint32_t kWfMaxWaveSpp = 16;        // so a wave holds at most 16 samples of a pixel
+// and about this many paths (80 B of state each).  Measured at 1080p, 1, 2, 4
+// and 8 samples per wave: brute force 41.9 / 36.6 / 35.0 / 36.3 ms per 64-spp
+// frame (fewer launches over thin deep-bounce queues), the LBVH 82.7 / 80.1 /
+// 89.6 / 99.3 ms per 16-spp frame (its traversal is L2-bound, and more path
+// state streaming through L2 evicts the tree).
+constexpr uint32_t kWfWavePathsBrute = 1u << 23;
+constexpr uint32_t kWfWavePathsBvh = 1u << 22;
+size_t wavefront_state_bytes(uint32_t npath);
+uint32_t wavefront_wave_spp(uint32_t npix, uint32_t spp, bool bvh);  // the wave's sample capacity W
 size_t wavefront_bvh_smem_bytes();
 cudaError_t wavefront_occupancy(bool bvh, int block, size_t smem, int* intersect_per_sm, int* shade_per_sm);
-cudaError_t wavefront_set_sample(uint32_t* sample, uint32_t v, cudaStream_t s);
+cudaError_t wavefront_set_word(uint32_t* word, uint32_t v, cudaStream_t s);
 cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s);
 
 // One scene of a batch (rdc_batch_upload): its view, accumulator, sample

@@ -13,12 +13,18 @@
 //                 one material class at a time (no divergence between the
 //                 glass, metal and rough branches of the scatter); survivors
 //                 are compacted into the next ray queue.
-// Accumulation must add a pixel's samples in sample order (the reference sums
-// sequentially, src/renderer/cpu.rs:198-210), so a wave is one sample index
-// for every pixel: generate, max_bounces x (intersect, shade), accumulate.
-// The wave is captured once as a CUDA graph and replayed per sample; the
-// sample index the RNG counter needs is read from device memory and advanced
-// by the accumulate kernel.  Results are bit-identical to render_kernel.
+// A wave is W consecutive sample indices of every pixel (W <= 16, sized so a
+// wave holds about 2^23 paths, 2^22 through the LBVH): generate, max_bounces x
+// (intersect, shade), accumulate.  Accumulation must add a pixel's samples in sample order (the
+// reference sums sequentially, src/renderer/cpu.rs:198-210), so the
+// accumulate kernel adds each pixel's W radiances in order.  The wave is
+// captured once as a CUDA graph and replayed; the first sample index and the
+// number of samples in the wave (W, or the remainder in the last wave) are
+// read from device memory, and the accumulate kernel advances the first.
+// Path state is a structure of arrays indexed by path = sub * npix + pixel,
+// sub the sample's place in the wave; a queue entry is (sub << 28) | pixel
+// (RDC_MAX_RESOLUTION^2 = 2^28 pixels).  Results are bit-identical to
+// render_kernel.
 #include <cstdint>
 
 #include "rdc_bvh.cuh"
@@ -34,19 +40,53 @@ __device__ __forceinline__ int material_class(const MatDev& m) {
     return 0;                        // the diffuse / specular draw
 }
 
+// Queue entries: the path's place in the wave (its sample's offset from the
+// wave's first) above kWfPixBits, its pixel below.
+__device__ __forceinline__ uint32_t wf_entry(uint32_t sub, uint32_t pix) { return (sub << kWfPixBits) | pix; }
+__device__ __forceinline__ uint32_t wf_pix(uint32_t e) { return e & ((1u << kWfPixBits) - 1u); }
+__device__ __forceinline__ uint32_t wf_sub(uint32_t e) { return e >> kWfPixBits; }
+
+// The pixel and the path (state index) a queue entry names.
+__device__ __forceinline__ void wf_decode(const WfParams& P, uint32_t e, uint32_t& pix, uint32_t& path) {
+    pix = (uint32_t)checked_index(P.sc.oob, wf_pix(e), P.npix);
+    path = (uint32_t)checked_index(P.sc.oob, (long long)wf_sub(e) * P.npix + pix, P.npath);
+}
+
+// grid (pixels / block, W): blockIdx.y is the sample's place in the wave
 __global__ void wf_generate(const WfParams P) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        P.counts[0] = P.max_bounces > 0 ? P.npix : 0u;
+    const uint32_t sub = blockIdx.y;
+    const uint32_t wn = *P.wave_n;
+    if (i == 0 && sub == 0) {
+        P.counts[0] = P.max_bounces > 0 ? P.npix * wn : 0u;
     }
-    if (i >= P.npix) return;
+    if (i >= P.npix || sub >= wn) return;
     V3 o, d;
     primary_ray(P.sc, i % P.sc.width, i / P.sc.width, o, d);
-    P.ox[i] = o.x; P.oy[i] = o.y; P.oz[i] = o.z;
-    P.dx[i] = d.x; P.dy[i] = d.y; P.dz[i] = d.z;
-    P.ar[i] = 1.0f; P.ag[i] = 1.0f; P.ab[i] = 1.0f;
-    P.lr[i] = 0.0f; P.lg[i] = 0.0f; P.lb[i] = 0.0f;
-    P.queue0[i] = i;
+    const uint32_t k = (uint32_t)checked_index(P.sc.oob, (long long)sub * P.npix + i, P.npath);
+    P.ox[k] = o.x; P.oy[k] = o.y; P.oz[k] = o.z;
+    P.dx[k] = d.x; P.dy[k] = d.y; P.dz[k] = d.z;
+    P.ar[k] = 1.0f; P.ag[k] = 1.0f; P.ab[k] = 1.0f;
+    P.lr[k] = 0.0f; P.lg[k] = 0.0f; P.lb[k] = 0.0f;
+    P.queue0[k] = wf_entry(sub, i);
+}
+
+// Append the lanes with cls >= 0 (their queue entry e) to the class queues,
+// one warp-aggregated atomic per class present.  Called by a full warp.
+__device__ __forceinline__ void wf_append_class(const WfParams& P, int cls, uint32_t e) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const unsigned m = __ballot_sync(FULL, cls == c);
+        if (m == 0u) continue;
+        const int leader = __ffs(m) - 1;
+        uint32_t b = 0;
+        if (lane == leader) b = atomicAdd(&P.counts[2 + c], (uint32_t)__popc(m));
+        b = __shfl_sync(FULL, b, leader);
+        if (cls == c)
+            P.cls[(size_t)c * P.npath + checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npath)] = e;
+    }
 }
 
 __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint32_t* __restrict__ q_in,
@@ -69,54 +109,28 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
     for (uint32_t wbase = base0; wbase < n; wbase += stride) {
         const uint32_t k = wbase + lane;
         int cls = -1;
-        uint32_t pix = 0;
+        uint32_t e = 0;
         if (k < n) {
-            pix = (uint32_t)checked_index(P.sc.oob, q_in[k], P.npix);
-            const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
-            const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
+            e = q_in[checked_index(P.sc.oob, k, P.npath)];
+            uint32_t pix, path;  // pix: unused here
+            wf_decode(P, e, pix, path);
+            const V3 o = mk(P.ox[path], P.oy[path], P.oz[path]);
+            const V3 d = mk(P.dx[path], P.dy[path], P.dz[path]);
             const RayPre r = ray_pre(o, d, P.sc.neg_zero);
             float t;
             int idx;
             intersect_all(s_rec, s_runs, (int)P.sc.nruns, scene_fast, r, t, idx);
-            P.hit_t[pix] = t;
-            P.hit_obj[pix] = idx;
+            P.hit_t[path] = t;
+            P.hit_obj[path] = idx;
             ++segs;
             cls = idx < 0 ? 3 : material_class(P.sc.mat[checked_index(P.sc.oob, idx, P.sc.nobj)]);
         }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const unsigned m = __ballot_sync(FULL, cls == c);
-            if (m == 0u) continue;
-            const int leader = __ffs(m) - 1;
-            uint32_t b = 0;
-            if (lane == leader) b = atomicAdd(&P.counts[2 + c], (uint32_t)__popc(m));
-            b = __shfl_sync(FULL, b, leader);
-            if (cls == c)
-                P.cls[(size_t)c * P.npix + checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npix)] = pix;
-        }
+        wf_append_class(P, cls, e);
     }
     unsigned long long s = segs;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(FULL, s, off);
     if (lane == 0 && s != 0ull) atomicAdd(P.segments, s);
-}
-
-// Append the lanes with cls >= 0 (their pixel pix) to the class queues,
-// one warp-aggregated atomic per class present.  Called by a full warp.
-__device__ __forceinline__ void wf_append_class(const WfParams& P, int cls, uint32_t pix) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const unsigned m = __ballot_sync(FULL, cls == c);
-        if (m == 0u) continue;
-        const int leader = __ffs(m) - 1;
-        uint32_t b = 0;
-        if (lane == leader) b = atomicAdd(&P.counts[2 + c], (uint32_t)__popc(m));
-        b = __shfl_sync(FULL, b, leader);
-        if (cls == c)
-            P.cls[(size_t)c * P.npix + checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npix)] = pix;
-    }
 }
 
 // LBVH scenes: the closest hit of every queued ray through the device LBVH,
@@ -145,14 +159,14 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
     T.bidx = -1;
     RayPre r;
     bool rfast = false, busy = false, pool_open = true;
-    uint32_t pix = 0, segs = 0;
+    uint32_t e = 0, path = 0, segs = 0;
     for (;;) {
         // lanes whose traversal is over: store the hit, queue the pixel by class
         const bool done = busy && T.cur < 0 && T.lmask == 0u;
         int cls = -1;
         if (done) {
-            P.hit_t[pix] = T.best;
-            P.hit_obj[pix] = T.bidx;
+            P.hit_t[path] = T.best;
+            P.hit_obj[path] = T.bidx;
             if (T.bidx < 0) {
                 cls = 3;
             } else {
@@ -162,7 +176,7 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
             }
             busy = false;
         }
-        if (__ballot_sync(FULL, done) != 0u) wf_append_class(P, cls, pix);
+        if (__ballot_sync(FULL, done) != 0u) wf_append_class(P, cls, e);
         // refill the idle lanes from the ray queue
         const unsigned idle = __ballot_sync(FULL, !busy);
         if (idle != 0u && pool_open) {
@@ -175,9 +189,11 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
             if (!busy) {
                 const uint32_t mine = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (mine < n) {
-                    pix = (uint32_t)checked_index(P.sc.oob, q_in[mine], P.npix);
-                    const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
-                    const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
+                    e = q_in[checked_index(P.sc.oob, mine, P.npath)];
+                    uint32_t pix;
+                    wf_decode(P, e, pix, path);
+                    const V3 o = mk(P.ox[path], P.oy[path], P.oz[path]);
+                    const V3 d = mk(P.dx[path], P.dy[path], P.dz[path]);
                     r = ray_pre(o, d, P.sc.neg_zero);
                     rfast = scene_fast && r.fast;
                     bvh_begin(P.bvh, r, rfast, T, cnt);
@@ -225,41 +241,43 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
     const int lane = threadIdx.x & 31;
     const uint32_t c0 = P.counts[2], c1 = P.counts[3], c2 = P.counts[4], c3 = P.counts[5];
     const uint32_t e0 = c0, e1 = e0 + c1, e2 = e1 + c2, total = e2 + c3;
-    const uint32_t sample = *P.sample;
+    const uint32_t sample0 = *P.sample;
     const bool more = bounce + 1u < P.max_bounces;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t base0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
     for (uint32_t wbase = base0; wbase < total; wbase += stride) {
         const uint32_t k = wbase + lane;
         bool requeue = false;
-        uint32_t pix = 0;
+        uint32_t e = 0;
         if (k < total) {
             const int c = k < e0 ? 0 : (k < e1 ? 1 : (k < e2 ? 2 : 3));
             const uint32_t pos = k - (c == 0 ? 0u : (c == 1 ? e0 : (c == 2 ? e1 : e2)));
-            pix = (uint32_t)checked_index(P.sc.oob, P.cls[(size_t)c * P.npix + checked_index(P.sc.oob, pos, P.npix)],
-                                          P.npix);
-            const V3 d = mk(P.dx[pix], P.dy[pix], P.dz[pix]);
-            V3 atten = mk(P.ar[pix], P.ag[pix], P.ab[pix]);
-            V3 light = mk(P.lr[pix], P.lg[pix], P.lb[pix]);
+            e = P.cls[(size_t)c * P.npath + checked_index(P.sc.oob, pos, P.npath)];
+            uint32_t pix, path;
+            wf_decode(P, e, pix, path);
+            const uint32_t sample = sample0 + wf_sub(e);
+            const V3 d = mk(P.dx[path], P.dy[path], P.dz[path]);
+            V3 atten = mk(P.ar[path], P.ag[path], P.ab[path]);
+            V3 light = mk(P.lr[path], P.lg[path], P.lb[path]);
             if (c == 3) {
                 // miss: the sky weighted by the throughput ends the path (cpu.rs:330-341)
                 const V3 sky = world_sample(P.sc, d);
                 light = vadd(light, mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z));
             } else {
-                const V3 o = mk(P.ox[pix], P.oy[pix], P.oz[pix]);
-                const int idx = (int)checked_index(P.sc.oob, P.hit_obj[pix], P.sc.nobj);
+                const V3 o = mk(P.ox[path], P.oy[path], P.oz[path]);
+                const int idx = (int)checked_index(P.sc.oob, P.hit_obj[path], P.sc.nobj);
                 const MatDev m = load_mat(P.sc.mat, idx);
-                const HitRec h = closest_hit(o, d, P.hit_t[pix], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
+                const HitRec h = closest_hit(o, d, P.hit_t[path], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
                 V3 no, nd;
                 scatter_drawn(d, h, m, pix, sample, bounce * 4u, P.stream_id, P.key0, P.key1, no, nd);
-                P.ox[pix] = no.x; P.oy[pix] = no.y; P.oz[pix] = no.z;
-                P.dx[pix] = nd.x; P.dy[pix] = nd.y; P.dz[pix] = nd.z;
+                P.ox[path] = no.x; P.oy[path] = no.y; P.oz[path] = no.z;
+                P.dx[path] = nd.x; P.dy[path] = nd.y; P.dz[path] = nd.z;
                 atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
                 light = vadd(light, mk(m.b.x, m.b.y, m.b.z));
-                P.ar[pix] = atten.x; P.ag[pix] = atten.y; P.ab[pix] = atten.z;
+                P.ar[path] = atten.x; P.ag[path] = atten.y; P.ab[path] = atten.z;
                 requeue = more;
             }
-            P.lr[pix] = light.x; P.lg[pix] = light.y; P.lb[pix] = light.z;
+            P.lr[path] = light.x; P.lg[path] = light.y; P.lb[path] = light.z;
         }
         const unsigned m = __ballot_sync(FULL, requeue);
         if (m != 0u) {
@@ -267,31 +285,44 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
             uint32_t b = 0;
             if (lane == leader) b = atomicAdd(n_out, (uint32_t)__popc(m));
             b = __shfl_sync(FULL, b, leader);
-            if (requeue) q_out[checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npix)] = pix;
+            if (requeue) q_out[checked_index(P.sc.oob, b + __popc(m & ((1u << lane) - 1u)), P.npath)] = e;
         }
     }
 }
 
+// Each pixel adds its wave's radiances in sample order.
 __global__ void wf_accumulate(const WfParams P) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t wn = *P.wave_n;
     if (i < P.npix) {
         float4 a = P.accum[i];
-        a.x = a.x + P.lr[i];
-        a.y = a.y + P.lg[i];
-        a.z = a.z + P.lb[i];
-        a.w = a.w + 1.0f;
+        for (uint32_t sub = 0; sub < wn; ++sub) {
+            const size_t k = (size_t)checked_index(P.sc.oob, (long long)sub * P.npix + i, P.npath);
+            a.x = a.x + P.lr[k];
+            a.y = a.y + P.lg[k];
+            a.z = a.z + P.lb[k];
+            a.w = a.w + 1.0f;
+        }
         P.accum[i] = a;
     }
-    if (i == 0) *P.sample += 1u;  // nothing in this launch reads it
+    if (i == 0) *P.sample += wn;  // nothing in this launch reads it
 }
 
-__global__ void wf_set_sample(uint32_t* sample, uint32_t v) { *sample = v; }
+__global__ void wf_set_word(uint32_t* word, uint32_t v) { *word = v; }
 
 }  // namespace
 
-size_t wavefront_state_bytes(uint32_t npix) {
-    // 12 state planes + t + obj + 2 ray queues + 4 class queues, 4 B each per pixel
-    return (size_t)npix * 4u * 20u;
+size_t wavefront_state_bytes(uint32_t npath) {
+    // 12 state planes + t + obj + 2 ray queues + 4 class queues, 4 B each per path
+    return (size_t)npath * 4u * 20u;
+}
+
+uint32_t wavefront_wave_spp(uint32_t npix, uint32_t spp, bool bvh) {
+    const uint32_t cap = bvh ? kWfWavePathsBvh : kWfWavePathsBrute;
+    uint32_t w = (npix == 0u || npix >= cap) ? 1u : cap / npix;
+    if (w > kWfMaxWaveSpp) w = kWfMaxWaveSpp;
+    if (w > spp) w = spp;
+    return w < 1u ? 1u : w;
 }
 
 size_t wavefront_bvh_smem_bytes() { return (size_t)kWfBvhBlock * kShortStack * sizeof(uint2); }
@@ -311,17 +342,18 @@ cudaError_t wavefront_occupancy(bool bvh, int block, size_t smem, int* intersect
     return e;
 }
 
-cudaError_t wavefront_set_sample(uint32_t* sample, uint32_t v, cudaStream_t s) {
-    wf_set_sample<<<1, 1, 0, s>>>(sample, v);
+cudaError_t wavefront_set_word(uint32_t* word, uint32_t v, cudaStream_t s) {
+    wf_set_word<<<1, 1, 0, s>>>(word, v);
     return cudaGetLastError();
 }
 
-// Enqueue one wave (one sample of every pixel) on s; captured into a graph by
-// the caller.  grid_i / grid_s: persistent grids of the two queue kernels
-// (the intersect kernel is wf_intersect_bvh when p.use_bvh).
+// Enqueue one wave (up to p.npath / p.npix samples of every pixel; *p.wave_n
+// of them) on s; captured into a graph by the caller.  grid_i / grid_s:
+// persistent grids of the two queue kernels (the intersect kernel is
+// wf_intersect_bvh when p.use_bvh).
 cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s) {
     const uint32_t b = 256, g = (p.npix + b - 1) / b;
-    wf_generate<<<g, b, 0, s>>>(p);
+    wf_generate<<<dim3(g, p.npath / p.npix), b, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     for (uint32_t bounce = 0; bounce < p.max_bounces && e == cudaSuccess; ++bounce) {
         uint32_t* q_in = (bounce & 1u) ? p.queue1 : p.queue0;

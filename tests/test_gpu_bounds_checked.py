@@ -63,8 +63,8 @@ c2 = resized(scenegen.c2_default().scene, 32, 18)
 run("brute", lambda: render("brute", c1, 2, 8, 5))
 run("benchmark_scene", lambda: render("benchmark_scene", bench, 1, 12, 6))
 run("lbvh", lambda: render("lbvh", big, 1, 6, 9, accel=native.ACCEL_LBVH))
-run("wavefront", lambda: render("wavefront", c2, 2, 12, 7, wavefront=True))
-run("wavefront_lbvh", lambda: render("wavefront_lbvh", big, 2, 8, 14, accel=native.ACCEL_LBVH, wavefront=True))
+run("wavefront", lambda: render("wavefront", c2, 19, 12, 7, wavefront=True))  # waves of 16 + 3 samples
+run("wavefront_lbvh", lambda: render("wavefront_lbvh", big, 18, 8, 14, accel=native.ACCEL_LBVH, wavefront=True))
 
 def batch():
     items = [(c1, 2, 6, 11), (resized(scenegen.c1_plain(seed=4).scene, 16, 16), 1, 4, 12)]
@@ -144,9 +144,9 @@ def test_checked_renders_equal_the_oracle(checked_run):
         ("brute", c1, 2, 8, 5, 0), ("static", c1, 2, 8, 5, 0),
         ("benchmark_scene", resized(Scene.load(GOLDEN / "benchmark.rscn"), 48, 27), 1, 12, 6, 0),
         ("lbvh", scenegen.c5_large(seed=3, width=24, height=16, n_spheres=600, n_cubes=60).scene, 1, 6, 9, 0),
-        ("wavefront", resized(scenegen.c2_default().scene, 32, 18), 2, 12, 7, 0),
+        ("wavefront", resized(scenegen.c2_default().scene, 32, 18), 19, 12, 7, 0),
         ("wavefront_lbvh", scenegen.c5_large(seed=3, width=24, height=16, n_spheres=600, n_cubes=60).scene,
-         2, 8, 14, 0),
+         18, 8, 14, 0),
         ("batch0", c1, 2, 6, 11, 0), ("batch1", resized(scenegen.c1_plain(seed=4).scene, 16, 16), 1, 4, 12, 1),
     ]
     for name, scene, spp, bounces, seed, stream in cases:

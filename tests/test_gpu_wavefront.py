@@ -1,6 +1,8 @@
 """Wavefront render (rdc_render_wavefront) against the megakernel (rdc_render):
 the same accumulator bit for bit and the same segment count, for the config
-scenes, a progressive split and the no-bounce case."""
+scenes, a progressive split, the no-bounce case and waves of several
+samples (full waves, a remainder, a first sample other than 0, an image
+whose wave holds fewer than 16 samples)."""
 import numpy as np
 import pytest
 
@@ -77,3 +79,20 @@ def test_wavefront_lbvh_on_small_scenes_and_refill_thresholds():
         if ref is None:
             (ref, _), _ = _both(scene, 0, 2, 12, 8, accel=native.ACCEL_LBVH)
         assert bits_equal(acc, ref), mi
+
+
+@pytest.mark.parametrize("w,h,s0,n,accel", [
+    (40, 24, 0, 37, native.ACCEL_BRUTE_FORCE),   # waves of 16, 16, 5
+    (40, 24, 5, 16, native.ACCEL_BRUTE_FORCE),   # one full wave from sample 5
+    (40, 24, 3, 17, native.ACCEL_LBVH),          # 16 + 1
+    (1024, 1024, 2, 11, native.ACCEL_BRUTE_FORCE),  # 2^20 pixels: waves of 8, 3
+    (1024, 512, 0, 15, native.ACCEL_LBVH),       # 2^19 pixels: waves of 8, 7 through the LBVH
+])
+def test_wavefront_waves_of_several_samples(w, h, s0, n, accel):
+    """A wave holds up to 16 consecutive samples of every pixel (about 2^23
+    paths, 2^22 through the LBVH) and adds each pixel's radiances in sample
+    order."""
+    scene = shrink(scenegen.c2_default().scene, w, h)
+    (a, sa), (b, sb) = _both(scene, s0, n, 6, 17, accel=accel)
+    assert sa == sb
+    assert bits_equal(a, b)
