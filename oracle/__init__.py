@@ -46,9 +46,9 @@ def load() -> C.CDLL:
     lib.oracle_uniforms.argtypes = [U32P, C.c_uint32, FP, FP]
     lib.oracle_uniforms.restype = None
     DP = C.POINTER(C.c_double)
-    lib.oracle_gradient.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, FP,
-                                    DP, DP, DP,
-                                    DP, C.c_int, C.POINTER(C.c_uint64), DP]
+    for fn in (lib.oracle_gradient, lib.oracle_gradient_f32):
+        fn.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, FP, DP, DP, DP, DP,
+                       C.c_int, C.POINTER(C.c_uint64), DP]
     _lib = lib
     return lib
 
@@ -77,13 +77,15 @@ def render(scene_c, s0, n, max_bounces, seed, accum=None, threads=1, stream=0):
     return acc, seg.value
 
 
-def gradient(scene_c, s0, n, max_bounces, seed, dl_dimage, threads=1, stream=0, pathwise=False):
+def gradient(scene_c, s0, n, max_bounces, seed, dl_dimage, threads=1, stream=0, pathwise=False, fp32=False):
     """FP64 reference gradient of sum(dl_dimage * image), image = mean radiance
     (HxWx3) of samples [s0, s0+n).  Returns (g_albedo Nx3, g_roughness N,
     g_emission Nx3, image HxWx3), all float64; with pathwise=True also the
     roughness gradient's pathwise part alone (N) as a fifth item (the part a
     small central difference with common random numbers sees when no coin
-    flips)."""
+    flips).  fp32=True: the same derivative with each path's intermediates
+    in float (the sums over paths in double), the precision the CUDA adjoint
+    works in."""
     lib = load()
     w, h = scene_c.desc.camera.resolution_x, scene_c.desc.camera.resolution_y
     nobj = scene_c.desc.object_count
@@ -95,9 +97,9 @@ def gradient(scene_c, s0, n, max_bounces, seed, dl_dimage, threads=1, stream=0, 
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     gp = np.zeros(nobj, np.float64)
     lost = C.c_uint64(0)
-    rc = lib.oracle_gradient(_desc(scene_c), s0, n, max_bounces, seed, stream, _f(dl), dp(ga), dp(gr),
-                             dp(ge),
-                             dp(img), threads, C.byref(lost), dp(gp))
+    fn = lib.oracle_gradient_f32 if fp32 else lib.oracle_gradient
+    rc = fn(_desc(scene_c), s0, n, max_bounces, seed, stream, _f(dl), dp(ga), dp(gr), dp(ge), dp(img), threads,
+            C.byref(lost), dp(gp))
     if rc != 0:
         raise RuntimeError(f"oracle_gradient failed ({rc})")
     gradient.lost_paths = lost.value

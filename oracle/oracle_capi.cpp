@@ -63,18 +63,19 @@ int oracle_render(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t 
     return 0;
 }
 
-// FP64 reference gradient (raydar_oracle_grad.hpp) of sum dL_dimage * image,
-// image = mean radiance (RGB) of samples [s0, s0+n).  Writes g_albedo (N*3),
-// g_rough (N), g_emission (N*3) and, if not null, image (npix*3).  Returns 1
-// on a bad argument, 2 when max_bounces exceeds the tangent slots.  lost_out
-// (may be null): paths whose double evaluation lost a recorded hit.
-int oracle_gradient(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed,
-                    uint32_t stream, const float* dl_dimage, double* g_albedo, double* g_rough,
-                    double* g_emission, double* image, int threads, uint64_t* lost_out, double* g_rough_path) {
+}  // extern "C"
+
+namespace {
+
+// The gradient of oracle_gradient / oracle_gradient_f32 with dual numbers D.
+template <typename D>
+int gradient_impl(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed,
+                  uint32_t stream, const float* dl_dimage, double* g_albedo, double* g_rough, double* g_emission,
+                  double* image, int threads, uint64_t* lost_out, double* g_rough_path) {
     if (!desc || !dl_dimage || !g_albedo || !g_rough || !g_emission || n == 0) return 1;
     if (max_bounces > (uint32_t)kGradSlots) return 2;
     const Scene<float> sf = scene_from_desc<float>(desc);
-    const Scene<Dual> s = scene_from_desc<Dual>(desc);
+    const Scene<D> s = scene_from_desc<D>(desc);
     std::atomic<uint64_t> lost{0};
     const uint32_t npix = s.width * s.height;
     const size_t nobj = s.objects.size();
@@ -119,6 +120,31 @@ int oracle_gradient(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_
     }
     if (lost_out) *lost_out = lost.load();
     return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// FP64 reference gradient (raydar_oracle_grad.hpp) of sum dL_dimage * image,
+// image = mean radiance (RGB) of samples [s0, s0+n).  Writes g_albedo (N*3),
+// g_rough (N), g_emission (N*3) and, if not null, image (npix*3).  Returns 1
+// on a bad argument, 2 when max_bounces exceeds the tangent slots.  lost_out
+// (may be null): paths whose double evaluation lost a recorded hit.
+int oracle_gradient(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed,
+                    uint32_t stream, const float* dl_dimage, double* g_albedo, double* g_rough,
+                    double* g_emission, double* image, int threads, uint64_t* lost_out, double* g_rough_path) {
+    return gradient_impl<Dual>(desc, s0, n, max_bounces, seed, stream, dl_dimage, g_albedo, g_rough, g_emission,
+                               image, threads, lost_out, g_rough_path);
+}
+
+// The same derivative with every per-path intermediate in float (DualF), the
+// precision of the CUDA adjoint; the sums over paths stay in double.
+int oracle_gradient_f32(const rdc_scene_desc* desc, uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed,
+                        uint32_t stream, const float* dl_dimage, double* g_albedo, double* g_rough,
+                        double* g_emission, double* image, int threads, uint64_t* lost_out, double* g_rough_path) {
+    return gradient_impl<DualF>(desc, s0, n, max_bounces, seed, stream, dl_dimage, g_albedo, g_rough, g_emission,
+                                image, threads, lost_out, g_rough_path);
 }
 
 // Same, for a list of pixel indices; accum holds npix*4 floats (in/out).

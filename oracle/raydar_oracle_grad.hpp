@@ -42,60 +42,70 @@ namespace oracle {
 
 constexpr int kGradSlots = 16;  // bounces with a roughness tangent slot each
 
-// Forward-mode dual number: a value and kGradSlots partial derivatives.
-struct Dual {
-    double v;
-    double d[kGradSlots];
-    Dual() : v(0.0) {
-        for (int i = 0; i < kGradSlots; ++i) d[i] = 0.0;
+// Forward-mode dual number: a value and kGradSlots partial derivatives, in R.
+// DualT<double> is the reference gradient.  DualT<float> evaluates the same
+// derivative with every intermediate in float, as the CUDA adjoint does: on a
+// path whose derivative is ill-conditioned (hits a few ulp apart inside one
+// object, where 1/t and grazing normals amplify rounding) the float and
+// double evaluations part ways, and the float one says what FP32 can give.
+// The operators are hidden friends, so the path code's implicit conversions
+// (T(2), x * 0.0001f) resolve as for a plain class.
+template <typename R>
+struct DualT {
+    R v;
+    R d[kGradSlots];
+    DualT() : v(R(0)) {
+        for (int i = 0; i < kGradSlots; ++i) d[i] = R(0);
     }
-    Dual(double x) : v(x) {  // NOLINT: implicit, as the path code writes T(2), T(0.0001f)
-        for (int i = 0; i < kGradSlots; ++i) d[i] = 0.0;
+    DualT(R x) : v(x) {  // NOLINT: implicit, as the path code writes T(2), T(0.0001f)
+        for (int i = 0; i < kGradSlots; ++i) d[i] = R(0);
     }
+
+    friend DualT operator+(const DualT& a, const DualT& b) {
+        DualT r(a.v + b.v);
+        for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] + b.d[i];
+        return r;
+    }
+    friend DualT operator-(const DualT& a, const DualT& b) {
+        DualT r(a.v - b.v);
+        for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] - b.d[i];
+        return r;
+    }
+    friend DualT operator-(const DualT& a) {
+        DualT r(-a.v);
+        for (int i = 0; i < kGradSlots; ++i) r.d[i] = -a.d[i];
+        return r;
+    }
+    friend DualT operator*(const DualT& a, const DualT& b) {
+        DualT r(a.v * b.v);
+        for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+        return r;
+    }
+    friend DualT operator/(const DualT& a, const DualT& b) {
+        DualT r(a.v / b.v);
+        const R inv = R(1) / b.v;
+        for (int i = 0; i < kGradSlots; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * inv;
+        return r;
+    }
+    friend bool operator<(const DualT& a, const DualT& b) { return a.v < b.v; }
+    friend bool operator<=(const DualT& a, const DualT& b) { return a.v <= b.v; }
+    friend bool operator>(const DualT& a, const DualT& b) { return a.v > b.v; }
+    friend bool operator>=(const DualT& a, const DualT& b) { return a.v >= b.v; }
+    friend bool operator==(const DualT& a, const DualT& b) { return a.v == b.v; }
+    friend bool operator!=(const DualT& a, const DualT& b) { return a.v != b.v; }
+
+    // Found by argument-dependent lookup from r_sqrt / r_fabs / r_signbit.
+    friend DualT sqrt(const DualT& a) {
+        DualT r(std::sqrt(a.v));
+        const R g = r.v > R(0) ? R(0.5) / r.v : R(0);
+        for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] * g;
+        return r;
+    }
+    friend DualT fabs(const DualT& a) { return std::signbit(a.v) ? -a : a; }
+    friend bool signbit(const DualT& a) { return std::signbit(a.v); }
 };
-
-inline Dual operator+(const Dual& a, const Dual& b) {
-    Dual r(a.v + b.v);
-    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] + b.d[i];
-    return r;
-}
-inline Dual operator-(const Dual& a, const Dual& b) {
-    Dual r(a.v - b.v);
-    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] - b.d[i];
-    return r;
-}
-inline Dual operator-(const Dual& a) {
-    Dual r(-a.v);
-    for (int i = 0; i < kGradSlots; ++i) r.d[i] = -a.d[i];
-    return r;
-}
-inline Dual operator*(const Dual& a, const Dual& b) {
-    Dual r(a.v * b.v);
-    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
-    return r;
-}
-inline Dual operator/(const Dual& a, const Dual& b) {
-    Dual r(a.v / b.v);
-    const double inv = 1.0 / b.v;
-    for (int i = 0; i < kGradSlots; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * inv;
-    return r;
-}
-inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
-inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
-inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
-inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
-inline bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
-inline bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
-
-// Found by argument-dependent lookup from r_sqrt / r_fabs / r_signbit.
-inline Dual sqrt(const Dual& a) {
-    Dual r(std::sqrt(a.v));
-    const double g = r.v > 0.0 ? 0.5 / r.v : 0.0;
-    for (int i = 0; i < kGradSlots; ++i) r.d[i] = a.d[i] * g;
-    return r;
-}
-inline Dual fabs(const Dual& a) { return std::signbit(a.v) ? -a : a; }
-inline bool signbit(const Dual& a) { return std::signbit(a.v); }
+using Dual = DualT<double>;
+using DualF = DualT<float>;
 
 // One path's discrete history on the float path: the object hit, its front
 // flag and the scatter choices per bounce, and whether it ended in a miss.
@@ -138,12 +148,14 @@ inline void record_path(const Scene<float>& s, Ray<float> ray, uint32_t max_boun
 }
 
 // A dual number with its value replaced and its tangents kept.
-inline Dual at_value(const Dual& a, double v) {
-    Dual r = a;
-    r.v = v;
+template <typename R>
+inline DualT<R> at_value(const DualT<R>& a, double v) {
+    DualT<R> r = a;
+    r.v = (R)v;
     return r;
 }
-inline V3<Dual> at_value(const V3<Dual>& a, V3<float> v) {
+template <typename R>
+inline V3<DualT<R>> at_value(const V3<DualT<R>>& a, V3<float> v) {
     return v3(at_value(a.x, v.x), at_value(a.y, v.y), at_value(a.z, v.z));
 }
 
@@ -160,36 +172,38 @@ inline V3<Dual> at_value(const V3<Dual>& a, V3<float> v) {
 // rays; they add no albedo or roughness term).
 // g_rough receives both roughness parts; g_rough_path (when not null) the
 // pathwise part alone.
-inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, uint32_t p0, uint32_t p1,
+// D: Dual (the reference) or DualF (the same derivative in float).
+template <typename D>
+inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<D>& s, uint32_t p0, uint32_t p1,
                                 uint32_t s0, uint32_t n, uint32_t max_bounces, uint64_t seed, uint32_t stream,
                                 const float* dl_dimage, double* g_albedo, double* g_rough, double* g_emission,
                                 double* image, double* g_rough_path = nullptr) {
     uint64_t lost = 0;
     for (uint32_t pix = p0; pix < p1; ++pix) {
         const Ray<float> prim_f = primary_ray(sf, pix % s.width, pix / s.width);
-        const Ray<Dual> prim = primary_ray(s, pix % s.width, pix / s.width);
+        const Ray<D> prim = primary_ray(s, pix % s.width, pix / s.width);
         double w[3], img[3] = {0.0, 0.0, 0.0};
         for (int c = 0; c < 3; ++c) w[c] = (double)dl_dimage[3 * (size_t)pix + c] / (double)n;
         for (uint32_t k = 0; k < n; ++k) {
             PathRecord rec;
             record_path(sf, prim_f, max_bounces, seed, stream, pix, s0 + k, &rec);
-            Ray<Dual> ray = prim;
+            Ray<D> ray = prim;
             bool ok = true;
             // d log P / d(slot j) of the coin that decided vertex v's lobe (0 without one)
             double dlogp[kGradSlots][kGradSlots];
             for (int v = 0; v < rec.nv && ok; ++v) {
-                Object<Dual> ob = s.objects[rec.obj[v]];
+                Object<D> ob = s.objects[rec.obj[v]];
                 // evaluate at the float path's ray and hit distance, with the
                 // tangents carried in double
                 ray.origin = at_value(ray.origin, rec.o[v]);
                 ray.direction = at_value(ray.direction, rec.d[v]);
-                Dual t;
+                D t;
                 if (!hit_object(ray, ob, &t)) {
                     ok = false;
                     break;
                 }
                 t = at_value(t, rec.t[v]);
-                Hit<Dual> h;
+                Hit<D> h;
                 h.index = rec.obj[v];
                 closest_hit(ray, t, ob, &h);
                 if (h.front != rec.front[v]) {  // grazing: keep the float path's side
@@ -199,15 +213,15 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
                 ob.roughness.d[v] = 1.0;  // tangent slot v: this bounce's roughness
                 uint32_t words[12];
                 bounce_words(seed, stream, pix, s0 + k, (uint32_t)v, words);
-                Ray<Dual> next;
-                Dual pc;
+                Ray<D> next;
+                D pc;
                 scatter(ray, h, ob, words, &next, &rec.ch[v], true, &pc);
-                for (int j = 0; j < kGradSlots; ++j) dlogp[v][j] = pc.d[j] / pc.v;
+                for (int j = 0; j < kGradSlots; ++j) dlogp[v][j] = (double)(pc.d[j] / pc.v);
                 ray = next;
             }
             double light[3] = {0.0, 0.0, 0.0};
             for (int v = 0; v < rec.nv; ++v) {
-                const Object<Dual>& ob = s.objects[rec.obj[v]];
+                const Object<D>& ob = s.objects[rec.obj[v]];
                 const double e[3] = {ob.emission_color.x.v * ob.emission_strength.v,
                                      ob.emission_color.y.v * ob.emission_strength.v,
                                      ob.emission_color.z.v * ob.emission_strength.v};
@@ -222,12 +236,12 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
             if (ok) {
                 double S[3] = {0.0, 0.0, 0.0};
                 if (rec.missed) {
-                    const V3<Dual> sky = world_sample(s, at_value(ray.direction, rec.d_end));
+                    const V3<D> sky = world_sample(s, at_value(ray.direction, rec.d_end));
                     const double sk[3] = {sky.x.v, sky.y.v, sky.z.v};
                     for (int c = 0; c < 3; ++c) {
                         double prod = 1.0;
                         for (int v = 0; v < rec.nv; ++v) {
-                            const V3<Dual>& a = s.objects[rec.obj[v]].albedo;
+                            const V3<D>& a = s.objects[rec.obj[v]].albedo;
                             prod *= c == 0 ? a.x.v : (c == 1 ? a.y.v : a.z.v);
                         }
                         S[c] = sk[c] * prod;
@@ -235,7 +249,7 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
                 }
                 for (int v = rec.nv - 1; v >= 0; --v) {
                     for (int c = 0; c < 3; ++c) after[v][c] = S[c];
-                    const Object<Dual>& ob = s.objects[rec.obj[v]];
+                    const Object<D>& ob = s.objects[rec.obj[v]];
                     S[0] += ob.emission_color.x.v * ob.emission_strength.v;
                     S[1] += ob.emission_color.y.v * ob.emission_strength.v;
                     S[2] += ob.emission_color.z.v * ob.emission_strength.v;
@@ -247,13 +261,13 @@ inline uint64_t gradient_pixels(const Scene<float>& sf, const Scene<Dual>& s, ui
                 }
             }
             if (rec.missed && ok) {
-                const V3<Dual> sky = world_sample(s, at_value(ray.direction, rec.d_end));
-                const Dual skyc[3] = {sky.x, sky.y, sky.z};
+                const V3<D> sky = world_sample(s, at_value(ray.direction, rec.d_end));
+                const D skyc[3] = {sky.x, sky.y, sky.z};
                 for (int c = 0; c < 3; ++c) {
                     double alb[kGradSlots];
                     double prod = 1.0;
                     for (int v = 0; v < rec.nv; ++v) {
-                        const V3<Dual>& a = s.objects[rec.obj[v]].albedo;
+                        const V3<D>& a = s.objects[rec.obj[v]].albedo;
                         alb[v] = c == 0 ? a.x.v : (c == 1 ? a.y.v : a.z.v);
                         prod *= alb[v];
                     }

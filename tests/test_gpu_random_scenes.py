@@ -151,29 +151,69 @@ def test_random_batch_matches_the_oracle(k):
         br.close()
 
 
-@pytest.mark.parametrize("k", range(24))
-def test_random_scene_adjoint_matches_the_fp64_oracle(k):
-    """rdc_backward on random scenes (1-16 bounces, both accelerations)
-    against the FP64 gradient oracle over the same paths, within the relative
-    L2 error of 1e-2 the gradients are specified with.  (dL/dimage is uniform
-    in [-1, 1], so an object's gradient is a sum of terms of both signs; the
-    FP32 atomic sums carry a rounding error relative to the terms' magnitudes,
-    which a sum that cancels can show as ~1e-3 of the total: measured up to
-    1.8e-3 on these scenes.)"""
+def _adjoint_case(k):
     scene, spp, _ = _random_scene(40000 + k)
     bounces = int(np.random.default_rng(k).choice([1, 3, 6, 16]))
-    seed = 300 + k
     dl = np.random.default_rng(60 + k).uniform(-1, 1, (scene.height, scene.width, 3)).astype(np.float32)
-    oa, orr, oe, _ = oracle.gradient(scene.to_c(), 0, spp, bounces, seed, dl, threads=8)
+    return scene, spp, bounces, 300 + k, dl
+
+
+def _adjoint(scene, s0, spp, bounces, seed, dl, accel):
+    r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
+    try:
+        r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
+        r.forward(scene, spp, spp_begin=s0)
+        return [np.asarray(g, np.float64) for g in r.backward(scene, dl)]
+    finally:
+        r.close()
+
+
+@pytest.mark.parametrize("k", range(200))
+def test_random_scene_adjoint_matches_the_oracle(k):
+    """rdc_backward on random scenes (1-16 bounces, both accelerations)
+    against the gradient oracle over the same paths, evaluated twice.  With
+    each path's intermediates in float (the adjoint's precision) the
+    relative L2 error must stay within 1e-4; in double, within the 1e-2 the
+    gradients are specified with, on every scene whose two evaluations agree
+    to 5e-3 and whose double replay kept every path.  The double evaluation
+    departs from the float one where a path's derivative is ill-conditioned
+    (hits a few ulp apart inside one object, where 1/t and grazing normals
+    amplify rounding) or where replaying a float path in double loses a
+    grazing hit (the oracle then drops that path): in 600 seeded scenes 13
+    such, 10 with lost paths; the adjoint matched the float evaluation in all
+    600 (worst 7e-6 relative, 2.6e-4 on a gradient of norm 5e-5).  (A float
+    sum that cancels can also differ from double by ~1e-3: measured up to
+    1.8e-3 on these scenes.)"""
+    scene, spp, bounces, seed, dl = _adjoint_case(k)
+    c = scene.to_c()
+    o64 = oracle.gradient(c, 0, spp, bounces, seed, dl, threads=8)[:3]
+    lost64 = oracle.gradient.lost_paths
+    o32 = oracle.gradient(c, 0, spp, bounces, seed, dl, threads=8, fp32=True)[:3]
+    assert oracle.gradient.lost_paths == 0  # the float replay is the float path itself
     for accel in (native.ACCEL_BRUTE_FORCE, native.ACCEL_LBVH):
-        r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
-        try:
-            r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
-            r.forward(scene, spp)
-            ga, gr, ge = r.backward(scene, dl)
-        finally:
-            r.close()
-        for name, g, o in (("albedo", ga, oa), ("roughness", gr, orr), ("emission", ge, oe)):
-            no = float(np.linalg.norm(o))
-            err = float(np.linalg.norm(np.asarray(g, np.float64) - o))
-            assert err <= 1e-2 * no + 1e-6, (k, accel, name, err, no)
+        g = _adjoint(scene, 0, spp, bounces, seed, dl, accel)
+        for name, gv, a, b in zip(("albedo", "roughness", "emission"), g, o64, o32):
+            n32, e32 = float(np.linalg.norm(b)), float(np.linalg.norm(gv - b))
+            assert e32 <= 1e-4 * n32 + 1e-6, (k, accel, name, "float", e32, n32)
+            n64, e64 = float(np.linalg.norm(a)), float(np.linalg.norm(gv - a))
+            if lost64 == 0 and float(np.linalg.norm(b - a)) <= 5e-3 * n64 + 1e-6:
+                assert e64 <= 1e-2 * n64 + 1e-6, (k, accel, name, "double", e64, n64)
+
+
+def test_an_ill_conditioned_path_follows_the_float_evaluation():
+    """Random scene 89, sample 2 of pixel (18, 27): a path of 11 vertices,
+    ten of them inside one partly metallic, partly transmissive object with
+    hits 2e-5 to 1e-4 apart.  The roughness derivative of the object its
+    first vertex hit is +1.66 in double and -0.88 in float; the adjoint
+    gives the float value, through either acceleration."""
+    scene, _, bounces, seed, dl = _adjoint_case(89)
+    one = np.zeros_like(dl)
+    one[27, 18] = dl[27, 18]
+    c = scene.to_c()
+    o64 = oracle.gradient(c, 2, 1, bounces, seed, one, threads=1)[1]
+    o32 = oracle.gradient(c, 2, 1, bounces, seed, one, threads=1, fp32=True)[1]
+    assert o64[43] > 1.0 and o32[43] < -0.5
+    for accel in (native.ACCEL_BRUTE_FORCE, native.ACCEL_LBVH):
+        gr = _adjoint(scene, 2, 1, bounces, seed, one, accel)[1]
+        assert abs(gr[43] - o32[43]) <= 1e-5 * abs(o32[43]), (accel, gr[43], o32[43], o64[43])
+        assert np.linalg.norm(gr - o32) <= 1e-4 * np.linalg.norm(o32)

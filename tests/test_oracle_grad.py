@@ -109,3 +109,16 @@ def test_lobe_choice_terms_are_separate_from_the_pathwise_part(setup):
     # objects with roughness 0 (glass) have no roughness gradient of either kind: d(r^2)/dr = 0 there
     glass = [i for i, o in enumerate(scene.objects) if o.material.roughness == 0.0]
     assert glass and all(gr[i] == 0.0 and gp[i] == 0.0 for i in glass)
+
+
+def test_the_float_evaluation_agrees_with_double_on_a_well_conditioned_scene(setup):
+    """oracle.gradient(fp32=True) takes the same derivative with each path's
+    intermediates in float (the precision of the CUDA adjoint).  On the c4
+    scene, where no path's derivative is ill-conditioned and the double
+    replay loses no hit, the two evaluations agree to float rounding
+    (measured 4e-5 relative on the roughness gradient, 6 bounces)."""
+    scene, dl, ga, gr, ge, img, _ = setup
+    fa, fr, fe, fimg = oracle.gradient(scene.to_c(), 0, SPP, BOUNCES, SEED, dl, threads=8, fp32=True)
+    assert oracle.gradient.lost_paths == 0
+    for f, d in ((fa, ga), (fr, gr), (fe, ge), (fimg, img)):
+        assert np.linalg.norm(f - d) <= 1e-4 * np.linalg.norm(d) + 1e-9
