@@ -657,7 +657,7 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
     static_assert((uint64_t)RDC_MAX_RESOLUTION * RDC_MAX_RESOLUTION <= (1ull << rdc::kWfPixBits),
                   "a queue entry holds any pixel index");
     static_assert(rdc::kWfMaxWaveSpp <= (1u << (32 - rdc::kWfPixBits)), "and any place in a wave");
-    const uint32_t wave = rdc::wavefront_wave_spp(npix, spp_count, ctx->bvh_active);
+    const uint32_t wave = rdc::wavefront_wave_spp(npix, spp_count);
     const uint32_t npath = npix * wave;
     if (rdc_status st = ensure(ctx, &ctx->d_wf, &ctx->cap_wf, rdc::wavefront_state_bytes(npath), "wavefront state"))
         return st;
@@ -681,12 +681,8 @@ rdc_status rdc_render_wavefront(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_c
                             : rdc::BvhView{nullptr, nullptr, 0, 0.0f, 0.0f, 0, nullptr};
     p.bvh_counters = ctx->d_counters + 2;
     p.min_idle = ctx->render_cfg.refill_min_idle;
-    float* f = reinterpret_cast<float*>(ctx->d_wf);
-    float** planes[12] = {&p.ox, &p.oy, &p.oz, &p.dx, &p.dy, &p.dz, &p.ar, &p.ag, &p.ab, &p.lr, &p.lg, &p.lb};
-    for (int i = 0; i < 12; ++i) *planes[i] = f + (size_t)i * npath;
-    p.hit_t = f + (size_t)12 * npath;
-    p.hit_obj = reinterpret_cast<int*>(f + (size_t)13 * npath);
-    uint32_t* u = reinterpret_cast<uint32_t*>(f + (size_t)14 * npath);
+    p.path = reinterpret_cast<rdc::WfPath*>(ctx->d_wf);  // device allocations are 256-byte aligned
+    uint32_t* u = reinterpret_cast<uint32_t*>(p.path + npath);
     p.queue0 = u;
     p.queue1 = u + npath;
     p.cls = u + 2 * (size_t)npath;

@@ -155,6 +155,18 @@ void reset_alloc_injection();
 
 // Wavefront render (rdc_wavefront.cu): per-pixel path state as planes of
 // npix floats in one buffer of wavefront_state_bytes(npix).
+// One path's state in the wavefront form, 64 B: the queue kernels take paths
+// in queue order, not path order, so a record per path makes each access one
+// or two whole sectors (as planes, each 4-byte field would pull a sector of
+// its own).
+struct alignas(16) WfPath {
+    float4 ot;  // the next ray's origin; w: its closest-hit distance
+    float4 dh;  // its direction; w: the hit object's index (int bits, -1 for none)
+    float4 atten;  // throughput (w unused)
+    float4 light;  // radiance gathered so far (w unused)
+};
+static_assert(sizeof(WfPath) == 64, "wavefront path record");
+
 struct WfParams {
     SceneView sc;
     float4* accum;
@@ -162,10 +174,7 @@ struct WfParams {
     uint32_t npath;     // paths a wave holds: npix x the wave's sample capacity W
     uint32_t* sample;   // the wave's first sample index (device), advanced per wave
     uint32_t* wave_n;   // samples in the current wave (device), W or the remainder in the last
-    float *ox, *oy, *oz, *dx, *dy, *dz;  // the path's next ray (npath entries each)
-    float *ar, *ag, *ab, *lr, *lg, *lb;  // throughput, radiance
-    float* hit_t;
-    int* hit_obj;
+    WfPath* path;               // npath records, one per path of the wave
     uint32_t *queue0, *queue1;  // ray queues of path entries, alternating per bounce
     uint32_t* cls;              // 4 class queues of npath entries: mix, metal, glass, miss
     uint32_t* counts;           // [0], [1] ray queue lengths, [2..5] class queue lengths, [6] the
@@ -183,15 +192,14 @@ constexpr int kWfBvhMinBlocks = 6;    // and the resident blocks its registers a
                                       // 64 registers measured 5% slower)
 constexpr uint32_t kWfPixBits = 28;          // a queue entry: the path's place in its wave << 28 | its pixel
 constexpr uint32_t kWfMaxWaveSpp = 16;        // so a wave holds at most 16 samples of a pixel
-// and about this many paths (80 B of state each).  Measured at 1080p, 1, 2, 4
-// and 8 samples per wave: brute force 41.9 / 36.6 / 35.0 / 36.3 ms per 64-spp
-// frame (fewer launches over thin deep-bounce queues), the LBVH 82.7 / 80.1 /
-// 89.6 / 99.3 ms per 16-spp frame (its traversal is L2-bound, and more path
-// state streaming through L2 evicts the tree).
-constexpr uint32_t kWfWavePathsBrute = 1u << 23;
-constexpr uint32_t kWfWavePathsBvh = 1u << 22;
+// and at most this many paths (88 B of state and queue entries each: 2.9 GB).
+// Measured at 1080p with 2, 4, 8 and 16 samples per wave: brute force 34.1 /
+// 30.7 / 29.4 / 29.0 ms per 64-spp frame (fewer launches over thin
+// deep-bounce queues), the LBVH 58.6 / 55.3 / 54.9 / 54.8 ms per 16-spp frame
+// (1 sample: 68.3 ms).
+constexpr uint32_t kWfWavePaths = 1u << 25;
 size_t wavefront_state_bytes(uint32_t npath);
-uint32_t wavefront_wave_spp(uint32_t npix, uint32_t spp, bool bvh);  // the wave's sample capacity W
+uint32_t wavefront_wave_spp(uint32_t npix, uint32_t spp);  // the wave's sample capacity W
 size_t wavefront_bvh_smem_bytes();
 cudaError_t wavefront_occupancy(bool bvh, int block, size_t smem, int* intersect_per_sm, int* shade_per_sm);
 cudaError_t wavefront_set_word(uint32_t* word, uint32_t v, cudaStream_t s);

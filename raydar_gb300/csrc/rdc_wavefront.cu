@@ -13,17 +13,16 @@
 //                 one material class at a time (no divergence between the
 //                 glass, metal and rough branches of the scatter); survivors
 //                 are compacted into the next ray queue.
-// A wave is W consecutive sample indices of every pixel (W <= 16, sized so a
-// wave holds about 2^23 paths, 2^22 through the LBVH): generate, max_bounces x
-// (intersect, shade), accumulate.  Accumulation must add a pixel's samples in sample order (the
+// A wave is W consecutive sample indices of every pixel (W <= 16 and at most
+// 2^25 paths): generate, max_bounces x (intersect, shade), accumulate.  Accumulation must add a pixel's samples in sample order (the
 // reference sums sequentially, src/renderer/cpu.rs:198-210), so the
 // accumulate kernel adds each pixel's W radiances in order.  The wave is
 // captured once as a CUDA graph and replayed; the first sample index and the
 // number of samples in the wave (W, or the remainder in the last wave) are
 // read from device memory, and the accumulate kernel advances the first.
-// Path state is a structure of arrays indexed by path = sub * npix + pixel,
-// sub the sample's place in the wave; a queue entry is (sub << 28) | pixel
-// (RDC_MAX_RESOLUTION^2 = 2^28 pixels).  Results are bit-identical to
+// Path state is one 64-byte record per path (WfPath), indexed by path =
+// sub * npix + pixel, sub the sample's place in the wave; a queue entry is
+// (sub << 28) | pixel (RDC_MAX_RESOLUTION^2 = 2^28 pixels).  Results are bit-identical to
 // render_kernel.
 #include <cstdint>
 
@@ -64,10 +63,11 @@ __global__ void wf_generate(const WfParams P) {
     V3 o, d;
     primary_ray(P.sc, i % P.sc.width, i / P.sc.width, o, d);
     const uint32_t k = (uint32_t)checked_index(P.sc.oob, (long long)sub * P.npix + i, P.npath);
-    P.ox[k] = o.x; P.oy[k] = o.y; P.oz[k] = o.z;
-    P.dx[k] = d.x; P.dy[k] = d.y; P.dz[k] = d.z;
-    P.ar[k] = 1.0f; P.ag[k] = 1.0f; P.ab[k] = 1.0f;
-    P.lr[k] = 0.0f; P.lg[k] = 0.0f; P.lb[k] = 0.0f;
+    WfPath& w = P.path[k];
+    w.ot = make_float4(o.x, o.y, o.z, 0.0f);
+    w.dh = make_float4(d.x, d.y, d.z, __int_as_float(-1));
+    w.atten = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.light = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     P.queue0[k] = wf_entry(sub, i);
 }
 
@@ -114,14 +114,13 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
             e = q_in[checked_index(P.sc.oob, k, P.npath)];
             uint32_t pix, path;  // pix: unused here
             wf_decode(P, e, pix, path);
-            const V3 o = mk(P.ox[path], P.oy[path], P.oz[path]);
-            const V3 d = mk(P.dx[path], P.dy[path], P.dz[path]);
-            const RayPre r = ray_pre(o, d, P.sc.neg_zero);
+            const float4 ot = P.path[path].ot, dh = P.path[path].dh;
+            const RayPre r = ray_pre(mk(ot.x, ot.y, ot.z), mk(dh.x, dh.y, dh.z), P.sc.neg_zero);
             float t;
             int idx;
             intersect_all(s_rec, s_runs, (int)P.sc.nruns, scene_fast, r, t, idx);
-            P.hit_t[path] = t;
-            P.hit_obj[path] = idx;
+            P.path[path].ot.w = t;
+            P.path[path].dh.w = __int_as_float(idx);
             ++segs;
             cls = idx < 0 ? 3 : material_class(P.sc.mat[checked_index(P.sc.oob, idx, P.sc.nobj)]);
         }
@@ -165,8 +164,8 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
         const bool done = busy && T.cur < 0 && T.lmask == 0u;
         int cls = -1;
         if (done) {
-            P.hit_t[path] = T.best;
-            P.hit_obj[path] = T.bidx;
+            P.path[path].ot.w = T.best;
+            P.path[path].dh.w = __int_as_float(T.bidx);
             if (T.bidx < 0) {
                 cls = 3;
             } else {
@@ -192,9 +191,8 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
                     e = q_in[checked_index(P.sc.oob, mine, P.npath)];
                     uint32_t pix;
                     wf_decode(P, e, pix, path);
-                    const V3 o = mk(P.ox[path], P.oy[path], P.oz[path]);
-                    const V3 d = mk(P.dx[path], P.dy[path], P.dz[path]);
-                    r = ray_pre(o, d, P.sc.neg_zero);
+                    const float4 ot = P.path[path].ot, dh = P.path[path].dh;
+                    r = ray_pre(mk(ot.x, ot.y, ot.z), mk(dh.x, dh.y, dh.z), P.sc.neg_zero);
                     rfast = scene_fast && r.fast;
                     bvh_begin(P.bvh, r, rfast, T, cnt);
                     busy = true;
@@ -256,28 +254,30 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
             uint32_t pix, path;
             wf_decode(P, e, pix, path);
             const uint32_t sample = sample0 + wf_sub(e);
-            const V3 d = mk(P.dx[path], P.dy[path], P.dz[path]);
-            V3 atten = mk(P.ar[path], P.ag[path], P.ab[path]);
-            V3 light = mk(P.lr[path], P.lg[path], P.lb[path]);
+            WfPath& w = P.path[path];
+            const float4 ot = w.ot, dh = w.dh, at4 = w.atten, li4 = w.light;
+            const V3 d = mk(dh.x, dh.y, dh.z);
+            V3 atten = mk(at4.x, at4.y, at4.z);
+            V3 light = mk(li4.x, li4.y, li4.z);
             if (c == 3) {
                 // miss: the sky weighted by the throughput ends the path (cpu.rs:330-341)
                 const V3 sky = world_sample(P.sc, d);
                 light = vadd(light, mk(sky.x * atten.x, sky.y * atten.y, sky.z * atten.z));
             } else {
-                const V3 o = mk(P.ox[path], P.oy[path], P.oz[path]);
-                const int idx = (int)checked_index(P.sc.oob, P.hit_obj[path], P.sc.nobj);
+                const V3 o = mk(ot.x, ot.y, ot.z);
+                const int idx = (int)checked_index(P.sc.oob, __float_as_int(dh.w), P.sc.nobj);
                 const MatDev m = load_mat(P.sc.mat, idx);
-                const HitRec h = closest_hit(o, d, P.hit_t[path], __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
+                const HitRec h = closest_hit(o, d, ot.w, __ldg(&P.sc.hit[idx]), __float_as_int(m.d.y));
                 V3 no, nd;
                 scatter_drawn(d, h, m, pix, sample, bounce * 4u, P.stream_id, P.key0, P.key1, no, nd);
-                P.ox[path] = no.x; P.oy[path] = no.y; P.oz[path] = no.z;
-                P.dx[path] = nd.x; P.dy[path] = nd.y; P.dz[path] = nd.z;
+                w.ot = make_float4(no.x, no.y, no.z, 0.0f);
+                w.dh = make_float4(nd.x, nd.y, nd.z, __int_as_float(-1));
                 atten = mk(atten.x * m.a.x, atten.y * m.a.y, atten.z * m.a.z);
                 light = vadd(light, mk(m.b.x, m.b.y, m.b.z));
-                P.ar[path] = atten.x; P.ag[path] = atten.y; P.ab[path] = atten.z;
+                w.atten = make_float4(atten.x, atten.y, atten.z, 0.0f);
                 requeue = more;
             }
-            P.lr[path] = light.x; P.lg[path] = light.y; P.lb[path] = light.z;
+            w.light = make_float4(light.x, light.y, light.z, 0.0f);
         }
         const unsigned m = __ballot_sync(FULL, requeue);
         if (m != 0u) {
@@ -298,9 +298,10 @@ __global__ void wf_accumulate(const WfParams P) {
         float4 a = P.accum[i];
         for (uint32_t sub = 0; sub < wn; ++sub) {
             const size_t k = (size_t)checked_index(P.sc.oob, (long long)sub * P.npix + i, P.npath);
-            a.x = a.x + P.lr[k];
-            a.y = a.y + P.lg[k];
-            a.z = a.z + P.lb[k];
+            const float4 li = P.path[k].light;
+            a.x = a.x + li.x;
+            a.y = a.y + li.y;
+            a.z = a.z + li.z;
             a.w = a.w + 1.0f;
         }
         P.accum[i] = a;
@@ -313,13 +314,12 @@ __global__ void wf_set_word(uint32_t* word, uint32_t v) { *word = v; }
 }  // namespace
 
 size_t wavefront_state_bytes(uint32_t npath) {
-    // 12 state planes + t + obj + 2 ray queues + 4 class queues, 4 B each per path
-    return (size_t)npath * 4u * 20u;
+    // a 64-byte record + 2 ray queues and 4 class queues of 4-byte entries per path
+    return (size_t)npath * (sizeof(WfPath) + 4u * 6u);
 }
 
-uint32_t wavefront_wave_spp(uint32_t npix, uint32_t spp, bool bvh) {
-    const uint32_t cap = bvh ? kWfWavePathsBvh : kWfWavePathsBrute;
-    uint32_t w = (npix == 0u || npix >= cap) ? 1u : cap / npix;
+uint32_t wavefront_wave_spp(uint32_t npix, uint32_t spp) {
+    uint32_t w = (npix == 0u || npix >= kWfWavePaths) ? 1u : kWfWavePaths / npix;
     if (w > kWfMaxWaveSpp) w = kWfMaxWaveSpp;
     if (w > spp) w = spp;
     return w < 1u ? 1u : w;

@@ -85,13 +85,12 @@ def test_wavefront_lbvh_on_small_scenes_and_refill_thresholds():
     (40, 24, 0, 37, native.ACCEL_BRUTE_FORCE),   # waves of 16, 16, 5
     (40, 24, 5, 16, native.ACCEL_BRUTE_FORCE),   # one full wave from sample 5
     (40, 24, 3, 17, native.ACCEL_LBVH),          # 16 + 1
-    (1024, 1024, 2, 11, native.ACCEL_BRUTE_FORCE),  # 2^20 pixels: waves of 8, 3
-    (1024, 512, 0, 15, native.ACCEL_LBVH),       # 2^19 pixels: waves of 8, 7 through the LBVH
+    (4096, 2048, 2, 11, native.ACCEL_BRUTE_FORCE),  # 2^23 pixels: waves of 4, 4, 3
+    (4096, 4096, 0, 3, native.ACCEL_LBVH),       # 2^24 pixels: waves of 2, 1 through the LBVH
 ])
 def test_wavefront_waves_of_several_samples(w, h, s0, n, accel):
-    """A wave holds up to 16 consecutive samples of every pixel (about 2^23
-    paths, 2^22 through the LBVH) and adds each pixel's radiances in sample
-    order."""
+    """A wave holds up to 16 consecutive samples of every pixel (at most 2^25
+    paths) and adds each pixel's radiances in sample order."""
     scene = shrink(scenegen.c2_default().scene, w, h)
     (a, sa), (b, sb) = _both(scene, s0, n, 6, 17, accel=accel)
     assert sa == sb
