@@ -310,12 +310,14 @@ rdc_status rdc_batch_get_config(rdc_ctx* ctx, rdc_launch_config* config);
  * Leaves the accumulators of the last trial; render again for results. */
 rdc_status rdc_batch_autotune(rdc_ctx* ctx, rdc_launch_config* best_out, float* best_ms_out);
 
-/* The same render as rdc_render, bit for bit, in wavefront form: per-pixel
- * path state in device memory, one launch per bounce for the closest hits of
- * all queued rays and one for shading them, regrouped by material class
+/* The same render as rdc_render, bit for bit, in wavefront form: per-path
+ * state in device memory, one launch per bounce for the closest hits of all
+ * queued rays and one for shading them, regrouped by material class
  * (diffuse/specular mix, metal, glass, miss) so each warp shades one class.
- * One wave is one sample of every pixel (a CUDA graph replayed per sample),
- * which keeps the per-pixel sample order of src/renderer/cpu.rs:198-210.
+ * One wave is up to 16 consecutive samples of every pixel, at most 2^25
+ * paths (88 bytes of device memory each: 2.9 GB at 1080p), a CUDA graph
+ * replayed per wave; each pixel adds its samples in sample order, as
+ * src/renderer/cpu.rs:198-210 does.
  * With an LBVH the closest hits come from a persistent kernel whose lanes
  * take queued rays as they finish their traversals (refill_min_idle of
  * rdc_set_render_config sets how many idle lanes trigger a refill).

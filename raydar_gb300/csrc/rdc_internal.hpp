@@ -153,8 +153,8 @@ void set_thread_error(const std::string& msg);
 cudaError_t dev_malloc(void** ptr, size_t bytes);
 void reset_alloc_injection();
 
-// Wavefront render (rdc_wavefront.cu): per-pixel path state as planes of
-// npix floats in one buffer of wavefront_state_bytes(npix).
+// Wavefront render (rdc_wavefront.cu): the path records and queues of one
+// wave in one buffer of wavefront_state_bytes(npath).
 // One path's state in the wavefront form, 64 B: the queue kernels take paths
 // in queue order, not path order, so a record per path makes each access one
 // or two whole sectors (as planes, each 4-byte field would pull a sector of
