@@ -3,7 +3,9 @@
 - RDC_MAX_RESOLUTION per axis (16384 x 16384, 268 M pixels, a 4.3 GB
   accumulator): every pixel's sample count, the segment count against the
   oracle's over the same frame at 1 bounce, and a pixel sample (corners,
-  edges, the last pixel, random ones) bit for bit at 3 bounces;
+  edges, the last pixel, random ones) bit for bit at 3 bounces; the
+  wavefront form at that size (one-sample waves of 2^28 paths, 23.6 GB of
+  path records and queues) equal to the megakernel;
 - RDC_MAX_BOUNCES (1024): paths that never escape a closed box run all their
   bounces, brute force and LBVH, bit-identical to the oracle;
 - RDC_MAX_BRUTE_OBJECTS (4096): brute force at the limit, its refusal one
@@ -50,6 +52,22 @@ def test_maximum_resolution():
     px = np.unique(np.concatenate([edge, rng.integers(0, n * n, 4000)])).astype(np.uint32)
     ref, _ = oracle.render_pixels(scene.to_c(), px, 0, 1, 3, 32)
     assert bits_equal(acc.reshape(-1, 4)[px], ref)
+
+
+def test_wavefront_at_the_maximum_resolution():
+    n = 16384
+    scene = resized(scenegen.c2_default().scene, n, n)
+    out = []
+    for fn in ("rdc_render", "rdc_render_wavefront"):
+        r = CudaRenderer(RendererConfig(max_bounces=2), seed=33)
+        r.upload(scene)
+        r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+        r._check(getattr(r.lib, fn)(r.ctx, 0, 1, 2, 33), fn)
+        out.append((r.accumulator(scene), r.stats().segments))
+        r.close()
+    (a, sa), (b, sb) = out
+    assert sa == sb and sa > n * n
+    assert bits_equal(a, b)
 
 
 def _closed_box(width=8, height=8):
