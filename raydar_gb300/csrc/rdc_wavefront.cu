@@ -2,28 +2,28 @@
 // the megakernel-vs-wavefront comparison.
 //
 // The megakernel (render_kernel) keeps each path in one lane's registers from
-// its primary ray to its end.  Here a path's state lives in HBM (structure of
-// arrays indexed by pixel) and every bounce is two launches over queues:
+// its primary ray to its end.  Here a path's state lives in HBM (one 64-byte
+// record per path) and every bounce is two launches over queues:
 //   wf_intersect  one thread per queued ray: the brute-force closest hit over
 //                 the scene staged in shared memory (the megakernel's
-//                 intersect_all), then the ray's pixel is appended to one of
-//                 four class queues -- diffuse/specular mix, metal, glass,
-//                 miss -- with one warp-aggregated atomic per class;
+//                 intersect_all), then the ray's queue entry is appended to
+//                 one of four class queues -- diffuse/specular mix, metal,
+//                 glass, miss -- with one warp-aggregated atomic per class;
 //   wf_shade      over the four class queues back to back, so a warp shades
 //                 one material class at a time (no divergence between the
 //                 glass, metal and rough branches of the scatter); survivors
 //                 are compacted into the next ray queue.
 // A wave is W consecutive sample indices of every pixel (W <= 16 and at most
-// 2^25 paths): generate, max_bounces x (intersect, shade), accumulate.  Accumulation must add a pixel's samples in sample order (the
-// reference sums sequentially, src/renderer/cpu.rs:198-210), so the
-// accumulate kernel adds each pixel's W radiances in order.  The wave is
-// captured once as a CUDA graph and replayed; the first sample index and the
-// number of samples in the wave (W, or the remainder in the last wave) are
-// read from device memory, and the accumulate kernel advances the first.
-// Path state is one 64-byte record per path (WfPath), indexed by path =
-// sub * npix + pixel, sub the sample's place in the wave; a queue entry is
-// (sub << 28) | pixel (RDC_MAX_RESOLUTION^2 = 2^28 pixels).  Results are bit-identical to
-// render_kernel.
+// 2^25 paths): generate, max_bounces x (intersect, shade), accumulate.
+// Accumulation must add a pixel's samples in sample order (the reference
+// sums sequentially, src/renderer/cpu.rs:198-210), so the accumulate kernel
+// adds each pixel's W radiances in order.  The wave is captured once as a
+// CUDA graph and replayed; the first sample index and the number of samples
+// in the wave (W, or the remainder in the last wave) are read from device
+// memory, and the accumulate kernel advances the first.  The records
+// (WfPath) are indexed by path = sub * npix + pixel, sub the sample's place
+// in the wave; a queue entry is (sub << 28) | pixel (RDC_MAX_RESOLUTION^2 =
+// 2^28 pixels).  Results are bit-identical to render_kernel.
 #include <cstdint>
 
 #include "rdc_bvh.cuh"
