@@ -127,6 +127,29 @@ def test_extreme_scale_scene_matches_the_oracle(k):
         assert bits_equal(acc, ref), (k, accel, len(scene.objects))
 
 
+@pytest.mark.parametrize("k", range(100))
+def test_random_scene_wavefront_in_several_waves_matches_the_oracle(k):
+    """The wavefront form with 17-40 samples (waves of 16 and a remainder)
+    from a first sample other than 0, through both accelerations."""
+    scene, _, bounces = _random_scene(80000 + k)
+    rng = np.random.default_rng(k)
+    s0, spp = int(rng.integers(0, 5)), int(rng.integers(17, 41))
+    seed = 500 + k
+    ref, segs = oracle.render(scene.to_c(), s0, spp, bounces, seed, threads=8)
+    for accel in (native.ACCEL_LBVH, native.ACCEL_BRUTE_FORCE):
+        r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
+        try:
+            r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
+            r.upload(scene)
+            r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+            r._check(r.lib.rdc_render_wavefront(r.ctx, s0, spp, bounces, seed), "rdc_render_wavefront")
+            acc, st = r.accumulator(scene), r.stats().segments
+        finally:
+            r.close()
+        assert st == segs, (k, accel)
+        assert bits_equal(acc, ref), (k, accel, len(scene.objects), spp)
+
+
 @pytest.mark.parametrize("k", range(48))
 def test_random_batch_matches_the_oracle(k):
     """A batch of 2-9 random scenes in one persistent launch: each equals the
