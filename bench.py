@@ -356,7 +356,7 @@ def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, he
     r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
     r.render_range(0, w.spp)  # warm-up frame
     r.stats()
-    segs = visits = tests = 0
+    segs = visits = tests = launches = 0
     dev_ms = 0.0
     t0 = time.perf_counter()
     for k in range(steps):
@@ -368,6 +368,7 @@ def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, he
         visits += st.node_visits
         tests += st.prim_tests
         dev_ms += st.device_ms
+        launches += st.kernel_launches
     wall = time.perf_counter() - t0
     r.close()
     v_per = visits / segs
@@ -386,6 +387,9 @@ def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, he
         "frac_of_peak": achieved / peak_tflops if peak_tflops else None,
         "bvh_build_s": build_s,
         "bvh_depth": depth,
+        # rdc_render's form (RDC_FORM_AUTO): the wavefront once a wave holds 4 or more samples of every pixel
+        "form": "wavefront" if launches > steps else "megakernel",
+        "kernel_launches_per_frame": launches / steps,
         "steps": steps,
     }
 
@@ -600,10 +604,12 @@ def progressive_bench(local: int, samples: int = 256, size: int = 584, bounces: 
 
 
 def _mk_vs_wf(local, w, spp, steps, accel=None):
-    from raydar_gb300 import CudaRenderer, RendererConfig
+    from raydar_gb300 import CudaRenderer, RendererConfig, native
     out = {}
     for fn in ("rdc_render", "rdc_render_wavefront"):
         r = CudaRenderer(RendererConfig(max_bounces=w.max_bounces), device=local, seed=0)
+        # the megakernel arm: rdc_render held to its megakernel form
+        r._check(r.lib.rdc_set_render_form(r.ctx, native.FORM_MEGAKERNEL), "rdc_set_render_form")
         if accel is not None:
             r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
         r.upload(w.scene)

@@ -65,6 +65,11 @@ enum { RDC_PROJECTION_PERSPECTIVE = 0, RDC_PROJECTION_ORTHOGRAPHIC = 1 };
 enum { RDC_ACCEL_AUTO = 0, RDC_ACCEL_BRUTE_FORCE = 1, RDC_ACCEL_LBVH = 2 };
 #define RDC_ACCEL_AUTO_LBVH_ABOVE 512u /* AUTO uses the LBVH above this many objects */
 
+/* The form rdc_render runs in (rdc_set_render_form).  Both give the same
+ * accumulator bit for bit. */
+enum { RDC_FORM_AUTO = 0, RDC_FORM_MEGAKERNEL = 1, RDC_FORM_WAVEFRONT = 2 };
+#define RDC_FORM_AUTO_WAVE_SAMPLES 4u /* AUTO: LBVH renders whose wave holds this many samples run as wavefront */
+
 /* Camera, field for field as src/scene/camera.rs:13-30.  The renderer uses
  * `position`, the resolution and the two inverse matrices as stored; the
  * remaining fields are carried so a caller can round-trip a Camera. */
@@ -216,6 +221,19 @@ rdc_status rdc_reset(rdc_ctx* ctx);
  * rdc_render(sample_count, 1). */
 rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count,
                       uint32_t max_bounces, uint64_t seed);
+
+/* Choose the form of later rdc_render calls (RDC_FORM_*): the megakernel
+ * (each path in one lane's registers), the wavefront form of
+ * rdc_render_wavefront, or AUTO (the default): the wavefront for LBVH scenes
+ * when one wave holds at least RDC_FORM_AUTO_WAVE_SAMPLES samples of every
+ * pixel (spp_count >= 4 and at most 2^23 pixels), else the megakernel.
+ * Measured on the 110k-object LBVH scene, wavefront / megakernel time:
+ * 1080p 16 spp 0.92, 4 spp 0.93, 1 spp 1.22; 512x512 64 spp 0.69; 480x270
+ * 32 spp 0.55.  Brute-force scenes render fastest as megakernel (wavefront
+ * 1.44x slower on the 81-object 1080p frame).  RDC_ERR_INVALID_ARGUMENT for
+ * another value.  Affects speed and device memory (the wavefront's state,
+ * up to 2.9 GB) only, never results. */
+rdc_status rdc_set_render_form(rdc_ctx* ctx, uint32_t form);
 
 /* Render without allocating any GPU memory.  For callers that cannot call
  * cudaMalloc -- an application whose device memory belongs to another

@@ -67,6 +67,7 @@ struct rdc_ctx {
     bool last_timed = false;
     uint32_t last_launches = 0;
     rdc_launch_config render_cfg{(uint32_t)rdc::kRenderBlock, 0, 16};
+    uint32_t render_form = RDC_FORM_AUTO;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
     // closest-hit acceleration
@@ -503,10 +504,22 @@ rdc_status rdc_reset(rdc_ctx* ctx) {
     return RDC_OK;
 }
 
+rdc_status rdc_set_render_form(rdc_ctx* ctx, uint32_t form) {
+    if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
+    if (form > RDC_FORM_WAVEFRONT) return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_set_render_form: unknown form");
+    ctx->render_form = form;
+    return RDC_OK;
+}
+
 rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint32_t max_bounces,
                       uint64_t seed) {
     if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_render: no scene uploaded");
+    const bool wavefront =
+        ctx->render_form == RDC_FORM_WAVEFRONT ||
+        (ctx->render_form == RDC_FORM_AUTO && ctx->bvh_active && spp_count > 0 &&
+         rdc::wavefront_wave_spp(ctx->width * ctx->height, spp_count) >= RDC_FORM_AUTO_WAVE_SAMPLES);
+    if (wavefront) return rdc_render_wavefront(ctx, spp_begin, spp_count, max_bounces, seed);
     if (max_bounces > RDC_MAX_BOUNCES) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: max_bounces above RDC_MAX_BOUNCES");
     if ((uint64_t)spp_begin + spp_count > 0xFFFFFFFFull)
         return fail(ctx, RDC_ERR_INVALID_ARGUMENT, "rdc_render: sample range overflows 32 bits");

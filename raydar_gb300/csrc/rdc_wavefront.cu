@@ -21,9 +21,13 @@
 // CUDA graph and replayed; the first sample index and the number of samples
 // in the wave (W, or the remainder in the last wave) are read from device
 // memory, and the accumulate kernel advances the first.  The records
-// (WfPath) are indexed by path = sub * npix + pixel, sub the sample's place
-// in the wave; a queue entry is (sub << 28) | pixel (RDC_MAX_RESOLUTION^2 =
-// 2^28 pixels).  Results are bit-identical to render_kernel.
+// (WfPath) are indexed by path = pixel * n + sub, n the wave's sample count
+// and sub the sample's place in the wave, and the first ray queue lists them
+// in that order: a warp's lanes start on a few pixels' samples, whose primary
+// rays are the same (the reference samples the pixel corner), and the first
+// bounces' rays start close together.  A queue entry is (sub << 28) | pixel
+// (RDC_MAX_RESOLUTION^2 = 2^28 pixels).  Results are bit-identical to
+// render_kernel.
 #include <cstdint>
 
 #include "rdc_bvh.cuh"
@@ -45,25 +49,28 @@ __device__ __forceinline__ uint32_t wf_entry(uint32_t sub, uint32_t pix) { retur
 __device__ __forceinline__ uint32_t wf_pix(uint32_t e) { return e & ((1u << kWfPixBits) - 1u); }
 __device__ __forceinline__ uint32_t wf_sub(uint32_t e) { return e >> kWfPixBits; }
 
-// The pixel and the path (state index) a queue entry names.
-__device__ __forceinline__ void wf_decode(const WfParams& P, uint32_t e, uint32_t& pix, uint32_t& path) {
+// The pixel and the path (record index) a queue entry names; wn: the
+// wave's sample count.
+__device__ __forceinline__ void wf_decode(const WfParams& P, uint32_t wn, uint32_t e, uint32_t& pix,
+                                          uint32_t& path) {
     pix = (uint32_t)checked_index(P.sc.oob, wf_pix(e), P.npix);
-    path = (uint32_t)checked_index(P.sc.oob, (long long)wf_sub(e) * P.npix + pix, P.npath);
+    path = (uint32_t)checked_index(P.sc.oob, (long long)pix * wn + wf_sub(e), P.npath);
 }
 
-// grid (pixels / block, W): blockIdx.y is the sample's place in the wave
+// One thread per record, in record order (a warp writes 32 consecutive
+// records: whole sectors; one thread per pixel writing its wn records, or
+// blocks per sample index, measured slower).
 __global__ void wf_generate(const WfParams P) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t sub = blockIdx.y;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t wn = *P.wave_n;
-    if (i == 0 && sub == 0) {
+    if (k == 0) {
         P.counts[0] = P.max_bounces > 0 ? P.npix * wn : 0u;
     }
-    if (i >= P.npix || sub >= wn) return;
+    if (k >= P.npix * wn) return;
+    const uint32_t i = k / wn, sub = k - i * wn;
     V3 o, d;
     primary_ray(P.sc, i % P.sc.width, i / P.sc.width, o, d);
-    const uint32_t k = (uint32_t)checked_index(P.sc.oob, (long long)sub * P.npix + i, P.npath);
-    WfPath& w = P.path[k];
+    WfPath& w = P.path[checked_index(P.sc.oob, k, P.npath)];
     w.ot = make_float4(o.x, o.y, o.z, 0.0f);
     w.dh = make_float4(d.x, d.y, d.z, __int_as_float(-1));
     w.atten = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
@@ -101,6 +108,7 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t n = *n_in;
+    const uint32_t wn = *P.wave_n;
     const bool scene_fast = P.sc.fast_div != 0u;
     uint32_t segs = 0;
     // warp-uniform trip count so the ballots below see whole warps
@@ -113,7 +121,7 @@ __global__ void __launch_bounds__(256) wf_intersect(const WfParams P, const uint
         if (k < n) {
             e = q_in[checked_index(P.sc.oob, k, P.npath)];
             uint32_t pix, path;  // pix: unused here
-            wf_decode(P, e, pix, path);
+            wf_decode(P, wn, e, pix, path);
             const float4 ot = P.path[path].ot, dh = P.path[path].dh;
             const RayPre r = ray_pre(mk(ot.x, ot.y, ot.z), mk(dh.x, dh.y, dh.z), P.sc.neg_zero);
             float t;
@@ -149,6 +157,7 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
     uint2 deep[kBvhStack - kShortStack];
     SplitStack stack{s_stack + threadIdx.x, blockDim.x, deep};
     const uint32_t n = *n_in;
+    const uint32_t wn = *P.wave_n;
     const bool scene_fast = P.sc.fast_div != 0u;
     BvhCounters cnt;
     BvhTrav T;
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(kWfBvhBlock, kWfBvhMinBlocks)
                 if (mine < n) {
                     e = q_in[checked_index(P.sc.oob, mine, P.npath)];
                     uint32_t pix;
-                    wf_decode(P, e, pix, path);
+                    wf_decode(P, wn, e, pix, path);
                     const float4 ot = P.path[path].ot, dh = P.path[path].dh;
                     r = ray_pre(mk(ot.x, ot.y, ot.z), mk(dh.x, dh.y, dh.z), P.sc.neg_zero);
                     rfast = scene_fast && r.fast;
@@ -240,6 +249,7 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
     const uint32_t c0 = P.counts[2], c1 = P.counts[3], c2 = P.counts[4], c3 = P.counts[5];
     const uint32_t e0 = c0, e1 = e0 + c1, e2 = e1 + c2, total = e2 + c3;
     const uint32_t sample0 = *P.sample;
+    const uint32_t wn = *P.wave_n;
     const bool more = bounce + 1u < P.max_bounces;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t base0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
@@ -252,7 +262,7 @@ __global__ void __launch_bounds__(256) wf_shade(const WfParams P, uint32_t bounc
             const uint32_t pos = k - (c == 0 ? 0u : (c == 1 ? e0 : (c == 2 ? e1 : e2)));
             e = P.cls[(size_t)c * P.npath + checked_index(P.sc.oob, pos, P.npath)];
             uint32_t pix, path;
-            wf_decode(P, e, pix, path);
+            wf_decode(P, wn, e, pix, path);
             const uint32_t sample = sample0 + wf_sub(e);
             WfPath& w = P.path[path];
             const float4 ot = w.ot, dh = w.dh, at4 = w.atten, li4 = w.light;
@@ -297,7 +307,7 @@ __global__ void wf_accumulate(const WfParams P) {
     if (i < P.npix) {
         float4 a = P.accum[i];
         for (uint32_t sub = 0; sub < wn; ++sub) {
-            const size_t k = (size_t)checked_index(P.sc.oob, (long long)sub * P.npix + i, P.npath);
+            const size_t k = (size_t)checked_index(P.sc.oob, (long long)i * wn + sub, P.npath);
             const float4 li = P.path[k].light;
             a.x = a.x + li.x;
             a.y = a.y + li.y;
@@ -352,8 +362,8 @@ cudaError_t wavefront_set_word(uint32_t* word, uint32_t v, cudaStream_t s) {
 // persistent grids of the two queue kernels (the intersect kernel is
 // wf_intersect_bvh when p.use_bvh).
 cudaError_t enqueue_wave(const WfParams& p, int grid_i, int grid_s, size_t smem, cudaStream_t s) {
-    const uint32_t b = 256, g = (p.npix + b - 1) / b;
-    wf_generate<<<dim3(g, p.npath / p.npix), b, 0, s>>>(p);
+    const uint32_t b = 256, g = (p.npix + b - 1) / b, gg = (p.npath + b - 1) / b;
+    wf_generate<<<gg, b, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     for (uint32_t bounce = 0; bounce < p.max_bounces && e == cudaSuccess; ++bounce) {
         uint32_t* q_in = (bounce & 1u) ? p.queue1 : p.queue0;

@@ -30,6 +30,7 @@ MAX_RESOLUTION = 16384
 MAX_OBJECTS = 1 << 24
 MAX_BRUTE_OBJECTS = 4096
 ACCEL_AUTO, ACCEL_BRUTE_FORCE, ACCEL_LBVH = 0, 1, 2
+FORM_AUTO, FORM_MEGAKERNEL, FORM_WAVEFRONT = 0, 1, 2
 MAX_BOUNCES = 1024
 
 F3 = C.c_float * 3
@@ -104,6 +105,7 @@ SIGNATURES = {
     "rdc_scene_upload": (C.c_int, [_P, C.POINTER(RdcSceneDesc)]),
     "rdc_reset": (C.c_int, [_P]),
     "rdc_set_accel": (C.c_int, [_P, C.c_uint32]),
+    "rdc_set_render_form": (C.c_int, [_P, C.c_uint32]),
     "rdc_render": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
     "rdc_render_static": (C.c_int, [C.POINTER(RdcSceneDesc), C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                     C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64), C.c_char_p, C.c_size_t]),

@@ -27,6 +27,10 @@ pub const RDC_PROJECTION_ORTHOGRAPHIC: u32 = 1;
 pub const RDC_ACCEL_AUTO: u32 = 0;
 pub const RDC_ACCEL_BRUTE_FORCE: u32 = 1;
 pub const RDC_ACCEL_LBVH: u32 = 2;
+pub const RDC_FORM_AUTO: u32 = 0;
+pub const RDC_FORM_MEGAKERNEL: u32 = 1;
+pub const RDC_FORM_WAVEFRONT: u32 = 2;
+pub const RDC_FORM_AUTO_WAVE_SAMPLES: u32 = 4;
 
 pub const RDC_MAX_RESOLUTION: u32 = 16384;
 pub const RDC_MAX_OBJECTS: u32 = 1 << 24;
@@ -156,6 +160,7 @@ extern "C" {
                                 length_out: *mut usize) -> rdc_status;
     pub fn rdc_scene_upload(ctx: *mut rdc_ctx, scene: *const rdc_scene_desc) -> rdc_status;
     pub fn rdc_set_accel(ctx: *mut rdc_ctx, mode: u32) -> rdc_status;
+    pub fn rdc_set_render_form(ctx: *mut rdc_ctx, form: u32) -> rdc_status;
     pub fn rdc_update_materials(ctx: *mut rdc_ctx, materials: *const rdc_material, count: u32) -> rdc_status;
 
     // rendering

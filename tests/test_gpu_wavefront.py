@@ -95,3 +95,44 @@ def test_wavefront_waves_of_several_samples(w, h, s0, n, accel):
     (a, sa), (b, sb) = _both(scene, s0, n, 6, 17, accel=accel)
     assert sa == sb
     assert bits_equal(a, b)
+
+
+def _render_form(scene, s0, n, bounces, seed, accel, form):
+    r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
+    try:
+        r._check(r.lib.rdc_set_render_form(r.ctx, form), "rdc_set_render_form")
+        r._check(r.lib.rdc_set_accel(r.ctx, accel), "rdc_set_accel")
+        r.upload(scene)
+        r._check(r.lib.rdc_reset(r.ctx), "rdc_reset")
+        r._check(r.lib.rdc_render(r.ctx, s0, n, bounces, seed), "rdc_render")
+        st = r.stats()
+        return r.accumulator(scene), st.segments, st.kernel_launches
+    finally:
+        r.close()
+
+
+@pytest.mark.parametrize("accel,spp,expect", [
+    (native.ACCEL_LBVH, 6, "wavefront"),      # a wave holds 6 samples: the wavefront
+    (native.ACCEL_LBVH, 3, "megakernel"),     # 3 samples per wave: the megakernel
+    (native.ACCEL_BRUTE_FORCE, 6, "megakernel"),
+])
+def test_rdc_render_chooses_its_form_and_every_form_agrees(accel, spp, expect):
+    """rdc_render in RDC_FORM_AUTO runs LBVH scenes as wavefront once a wave
+    holds 4 or more samples of every pixel, and everything else as
+    megakernel; the forced forms give the same accumulator."""
+    scene = shrink(scenegen.c2_default().scene, 48, 27)
+    auto, s_auto, l_auto = _render_form(scene, 1, spp, 8, 19, accel, native.FORM_AUTO)
+    assert (l_auto > 1) == (expect == "wavefront"), l_auto
+    for form in (native.FORM_MEGAKERNEL, native.FORM_WAVEFRONT):
+        acc, segs, launches = _render_form(scene, 1, spp, 8, 19, accel, form)
+        assert (launches == 1) == (form == native.FORM_MEGAKERNEL)
+        assert segs == s_auto and bits_equal(acc, auto), form
+
+
+def test_rdc_set_render_form_rejects_an_unknown_form():
+    r = CudaRenderer(RendererConfig(), seed=0)
+    try:
+        assert r.lib.rdc_set_render_form(r.ctx, 3) == 1  # RDC_ERR_INVALID_ARGUMENT
+        assert r.lib.rdc_set_render_form(None, native.FORM_AUTO) == 1
+    finally:
+        r.close()
