@@ -7,7 +7,8 @@
   wavefront form at that size (one-sample waves of 2^28 paths, 23.6 GB of
   path records and queues) equal to the megakernel;
 - RDC_MAX_BOUNCES (1024): paths that never escape a closed box run all their
-  bounces, brute force and LBVH, bit-identical to the oracle;
+  bounces, brute force, LBVH and the wavefront form, bit-identical to the
+  oracle;
 - RDC_MAX_BRUTE_OBJECTS (4096): brute force at the limit, its refusal one
   object above it, and the LBVH on the same scenes;
 - RDC_MAX_OBJECTS (2^24): the LBVH build and traversal against the oracle's
@@ -86,6 +87,17 @@ def test_maximum_bounces_in_a_closed_box(accel):
     acc, st = _render(scene, 2, 1024, 41, accel)
     ref, segs = oracle.render(scene.to_c(), 0, 2, 1024, 41, threads=8)
     assert st.segments == segs == 8 * 8 * 2 * 1024
+    assert bits_equal(acc, ref)
+
+
+def test_maximum_bounces_in_the_wavefront_form():
+    """1024 bounces through the LBVH at 5 samples: rdc_render takes the
+    wavefront form (a graph of 2 x 1024 queue launches per wave)."""
+    scene = _closed_box()
+    acc, st = _render(scene, 5, 1024, 43, native.ACCEL_LBVH)
+    assert st.kernel_launches > 2 * 1024
+    ref, segs = oracle.render(scene.to_c(), 0, 5, 1024, 43, threads=8)
+    assert st.segments == segs == 8 * 8 * 5 * 1024
     assert bits_equal(acc, ref)
 
 
