@@ -60,6 +60,8 @@ def _args():
     p.add_argument("--no-large", action="store_true", help="skip the LBVH (config 5) measurement")
     p.add_argument("--large-only", default="", metavar="WxHxSPP",
                    help="only the LBVH (config 5) measurement, at WxHxSPP (e.g. 480x270x32; 0 = full size)")
+    p.add_argument("--form", choices=("auto", "megakernel", "wavefront"), default="auto",
+                   help="rdc_render's form in the LBVH measurement (rdc_set_render_form; default: auto)")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (config 4) measurement")
     p.add_argument("--adjoint-only", action="store_true", help="only the adjoint (config 4) measurement")
     p.add_argument("--no-wavefront", action="store_true", help="skip the megakernel / wavefront A/B")
@@ -336,7 +338,8 @@ def batch_bench(local: int, steps: int, spp_div: int = 1):
     }
 
 
-def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, height: int = 1080, spp: int = 0):
+def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, height: int = 1080, spp: int = 0,
+               form: str = "auto"):
     """Config 5 forward: 100k spheres + 10k cubes, device-built LBVH, one
     1920x1080 frame of 256 spp / 12 bounces per step (width, height, spp:
     a smaller case of the same scene).  Ops/segment follow the LBVH model
@@ -348,6 +351,8 @@ def lbvh_bench(local: int, steps: int, peak_tflops: float, width: int = 1920, he
     if spp:
         w.spp = spp
     r = CudaRenderer(RendererConfig(max_sample_count=w.spp, max_bounces=w.max_bounces), device=local, seed=0)
+    forms = {"auto": native.FORM_AUTO, "megakernel": native.FORM_MEGAKERNEL, "wavefront": native.FORM_WAVEFRONT}
+    r._check(r.lib.rdc_set_render_form(r.ctx, forms[form]), "rdc_set_render_form")
     t0 = time.perf_counter()
     r.upload(w.scene)
     build_s = time.perf_counter() - t0
@@ -826,7 +831,7 @@ def run_ours(args):
     large = None
     if rank == 0 and not args.no_large:
         pk = max(ops_s.value / 1e12, n_sms * 128 * (clk.get("sm_mhz") or 0.0) * 1e6 / 1e12)
-        large = lbvh_bench(local, max(1, min(args.steps, 2)), pk)
+        large = lbvh_bench(local, max(1, min(args.steps, 2)), pk, form=args.form)
 
     adjoint = None
     if rank == 0 and not args.no_adjoint:
@@ -918,7 +923,7 @@ def main():
         import torch
         torch.cuda.set_device(_dist()[2])
         wh = [int(x) for x in args.large_only.split("x")] if args.large_only != "0" else [1920, 1080, 0]
-        print(json.dumps({"large_scene": lbvh_bench(_dist()[2], max(1, min(args.steps, 2)), 0.0, *wh)}))
+        print(json.dumps({"large_scene": lbvh_bench(_dist()[2], max(1, min(args.steps, 2)), 0.0, *wh, form=args.form)}))
         return
     if args.wavefront_only:
         import torch
