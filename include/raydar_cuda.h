@@ -223,16 +223,18 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count,
                       uint32_t max_bounces, uint64_t seed);
 
 /* Choose the form of later rdc_render calls (RDC_FORM_*): the megakernel
- * (each path in one lane's registers), the wavefront form of
- * rdc_render_wavefront, or AUTO (the default): the wavefront for LBVH scenes
- * when one wave holds at least RDC_FORM_AUTO_WAVE_SAMPLES samples of every
- * pixel (spp_count >= 4 and at most 2^23 pixels), else the megakernel.
- * Measured on the 110k-object LBVH scene, wavefront / megakernel time:
- * 1080p 16 spp 0.92, 4 spp 0.93, 1 spp 1.22; 512x512 64 spp 0.69; 480x270
- * 32 spp 0.55.  Brute-force scenes render fastest as megakernel (wavefront
- * 1.44x slower on the 81-object 1080p frame).  RDC_ERR_INVALID_ARGUMENT for
- * another value.  Affects speed and device memory (the wavefront's state,
- * up to 2.9 GB) only, never results. */
+ * (each path in one lane's registers, each lane owning whole pixels), the
+ * wavefront form of rdc_render_wavefront, or AUTO (the default): the
+ * wavefront when one wave holds at least RDC_FORM_AUTO_WAVE_SAMPLES samples
+ * of every pixel (spp_count >= 4 and at most 2^23 pixels) and the scene
+ * uses the LBVH or the image has at most 1.5 pixels per resident megakernel
+ * lane (1.5 x SMs x 768: 175,104 on 152 SMs), else the megakernel.
+ * Measured, wavefront / megakernel time: 110k-object LBVH scene at 1080p 16
+ * spp 0.92, 4 spp 0.93, 1 spp 1.22, at 512x512 64 spp 0.69, at 480x270 32
+ * spp 0.55; 81-object brute-force scene at 1080p 64 spp 1.46, 960x540 1.06,
+ * 480x270 0.63, 320x180 0.48, 128x72 at 512 spp 0.31.
+ * RDC_ERR_INVALID_ARGUMENT for another value.  Affects speed and device
+ * memory (the wavefront's state, up to 2.9 GB) only, never results. */
 rdc_status rdc_set_render_form(rdc_ctx* ctx, uint32_t form);
 
 /* Render without allocating any GPU memory.  For callers that cannot call

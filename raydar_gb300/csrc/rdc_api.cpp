@@ -515,10 +515,15 @@ rdc_status rdc_render(rdc_ctx* ctx, uint32_t spp_begin, uint32_t spp_count, uint
                       uint64_t seed) {
     if (!ctx) return RDC_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, RDC_ERR_NO_SCENE, "rdc_render: no scene uploaded");
+    // AUTO: the wavefront once a wave holds RDC_FORM_AUTO_WAVE_SAMPLES samples of every pixel, for LBVH
+    // scenes at any size and for brute-force images of at most 1.5 pixels per resident megakernel lane (with
+    // fewer pixels than that the megakernel's lanes, each owning whole pixels, run out of work early)
+    const uint64_t npix = (uint64_t)ctx->width * ctx->height;
+    const uint64_t lanes = (uint64_t)ctx->num_sms * rdc::kRenderBlock * rdc::kRenderBlocksPerSm;
     const bool wavefront =
         ctx->render_form == RDC_FORM_WAVEFRONT ||
-        (ctx->render_form == RDC_FORM_AUTO && ctx->bvh_active && spp_count > 0 &&
-         rdc::wavefront_wave_spp(ctx->width * ctx->height, spp_count) >= RDC_FORM_AUTO_WAVE_SAMPLES);
+        (ctx->render_form == RDC_FORM_AUTO && spp_count > 0 && (ctx->bvh_active || 2 * npix <= 3 * lanes) &&
+         rdc::wavefront_wave_spp((uint32_t)npix, spp_count) >= RDC_FORM_AUTO_WAVE_SAMPLES);
     if (wavefront) return rdc_render_wavefront(ctx, spp_begin, spp_count, max_bounces, seed);
     if (max_bounces > RDC_MAX_BOUNCES) return fail(ctx, RDC_ERR_LIMIT, "rdc_render: max_bounces above RDC_MAX_BOUNCES");
     if ((uint64_t)spp_begin + spp_count > 0xFFFFFFFFull)

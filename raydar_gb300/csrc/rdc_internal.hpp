@@ -269,6 +269,7 @@ inline bool sphere_fast_ok(const float c[3], float radius) {
 }
 
 constexpr int kRenderBlock = 256;
+constexpr int kRenderBlocksPerSm = 3;  // render_kernel's launch bound (80 registers)
 constexpr int kRenderBvhBlock = 128;  // largest block of render_bvh_kernel
 constexpr int kProbeChains = 8;  // independent FFMA chains per thread in the FP32 probe
 

@@ -83,7 +83,7 @@ __device__ __forceinline__ void add_warp_sum(unsigned long long* dst, unsigned l
 }
 
 // Brute force: the scene's records are staged in shared memory per block.
-__global__ void __launch_bounds__(kRenderBlock, 3) render_kernel(const RenderParams P) {
+__global__ void __launch_bounds__(kRenderBlock, kRenderBlocksPerSm) render_kernel(const RenderParams P) {
     extern __shared__ float4 smem[];
     __shared__ __align__(8) uint64_t s_bar;
     float4* s_rec = smem;

@@ -29,10 +29,15 @@ def golden_dir():
     return GOLDEN
 
 
-@pytest.fixture()
-def renderer():
-    """A CudaRenderer on device 0 (gpu tests only)."""
-    from raydar_gb300 import CudaRenderer, RendererConfig
+@pytest.fixture(params=["megakernel", "wavefront"])
+def renderer(request):
+    """A CudaRenderer on device 0 (gpu tests only) whose rdc_render is held to
+    one form, so the parity tests run through the megakernel and through the
+    wavefront form alike (RDC_FORM_AUTO would pick the wavefront for most of
+    their small images)."""
+    from raydar_gb300 import CudaRenderer, RendererConfig, native
     r = CudaRenderer(RendererConfig(), device=0, seed=0)
+    form = native.FORM_MEGAKERNEL if request.param == "megakernel" else native.FORM_WAVEFRONT
+    r._check(r.lib.rdc_set_render_form(r.ctx, form), "rdc_set_render_form")
     yield r
     r.close()

@@ -16,6 +16,7 @@ def _both(scene, s0, n, bounces, seed, accel=None):
     out = []
     for fn in ("rdc_render", "rdc_render_wavefront"):
         r = CudaRenderer(RendererConfig(max_bounces=bounces), seed=seed)
+        r._check(r.lib.rdc_set_render_form(r.ctx, native.FORM_MEGAKERNEL), "rdc_set_render_form")
         if accel is not None:
             r._check(r.lib.rdc_set_accel(r.ctx, accel), "set_accel")
         r.upload(scene)
@@ -111,16 +112,20 @@ def _render_form(scene, s0, n, bounces, seed, accel, form):
         r.close()
 
 
-@pytest.mark.parametrize("accel,spp,expect", [
-    (native.ACCEL_LBVH, 6, "wavefront"),      # a wave holds 6 samples: the wavefront
-    (native.ACCEL_LBVH, 3, "megakernel"),     # 3 samples per wave: the megakernel
-    (native.ACCEL_BRUTE_FORCE, 6, "megakernel"),
+@pytest.mark.parametrize("accel,w,h,spp,expect", [
+    (native.ACCEL_LBVH, 48, 27, 6, "wavefront"),          # a wave holds 6 samples: the wavefront
+    (native.ACCEL_LBVH, 48, 27, 3, "megakernel"),         # 3 samples per wave: the megakernel
+    (native.ACCEL_BRUTE_FORCE, 48, 27, 6, "wavefront"),   # a small image: the wavefront
+    (native.ACCEL_BRUTE_FORCE, 48, 27, 3, "megakernel"),
+    (native.ACCEL_BRUTE_FORCE, 640, 360, 4, "megakernel"),  # 230k pixels, above 1.5 per resident lane
+    (native.ACCEL_LBVH, 640, 360, 4, "wavefront"),
 ])
-def test_rdc_render_chooses_its_form_and_every_form_agrees(accel, spp, expect):
-    """rdc_render in RDC_FORM_AUTO runs LBVH scenes as wavefront once a wave
-    holds 4 or more samples of every pixel, and everything else as
-    megakernel; the forced forms give the same accumulator."""
-    scene = shrink(scenegen.c2_default().scene, 48, 27)
+def test_rdc_render_chooses_its_form_and_every_form_agrees(accel, w, h, spp, expect):
+    """rdc_render in RDC_FORM_AUTO runs a scene as wavefront once a wave holds
+    4 or more samples of every pixel and the scene uses the LBVH or the image
+    has at most 1.5 pixels per resident megakernel lane, and as megakernel
+    otherwise; the forced forms give the same accumulator."""
+    scene = shrink(scenegen.c2_default().scene, w, h)
     auto, s_auto, l_auto = _render_form(scene, 1, spp, 8, 19, accel, native.FORM_AUTO)
     assert (l_auto > 1) == (expect == "wavefront"), l_auto
     for form in (native.FORM_MEGAKERNEL, native.FORM_WAVEFRONT):
