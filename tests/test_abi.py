@@ -185,6 +185,28 @@ def test_the_cuda_backend_uses_only_declared_entry_points_and_the_patch_wires_it
     assert touched == {"Cargo.toml", "src/renderer/mod.rs", "src/cli/mod.rs", "src/main.rs"}
 
 
+def test_enum_constants_agree_across_the_header_and_both_bindings():
+    """RDC_ACCEL_* and RDC_FORM_* (and RDC_FORM_AUTO_WAVE_SAMPLES) have the
+    same values in include/raydar_cuda.h, the ctypes binding and the Rust
+    crate."""
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "raydar_cuda.h").read_text(), flags=re.S)
+    header = {}
+    for body in re.findall(r"enum\s*\{([^}]*)\}", text):
+        for name, val in re.findall(r"(RDC_(?:ACCEL|FORM)_[A-Z_]+)\s*=\s*(\d+)", body):
+            header[name] = int(val)
+    header.update({n: int(v) for n, v in re.findall(r"#define\s+(RDC_FORM_AUTO_WAVE_SAMPLES)\s+(\d+)u", text)})
+    assert {"RDC_ACCEL_AUTO", "RDC_ACCEL_LBVH", "RDC_FORM_AUTO", "RDC_FORM_MEGAKERNEL", "RDC_FORM_WAVEFRONT",
+            "RDC_FORM_AUTO_WAVE_SAMPLES"} <= set(header)
+    rust = {n: int(v) for n, v in re.findall(r"pub const (RDC_(?:ACCEL|FORM)_[A-Z_]+): u32 = (\d+);",
+                                               RUST_SYS.read_text())}
+    for name, val in header.items():
+        assert rust.get(name) == val, name
+        py = getattr(native, name[len("RDC_"):], None)
+        if py is not None:
+            assert py == val, name
+    assert native.FORM_WAVEFRONT == header["RDC_FORM_WAVEFRONT"] and native.ACCEL_LBVH == header["RDC_ACCEL_LBVH"]
+
+
 def test_version_string():
     assert b"sm_103a" in native.load().rdc_version()
 
